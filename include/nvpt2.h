@@ -1,0 +1,143 @@
+/*
+ * nvpt2.h - C ABI of the GB300 (sm_103a) Koopmans-matrix and SC/PC-NEVPT2 library.
+ *
+ * Drop-in boundary for the compute subroutines of qcscine/nevpt2's two
+ * Fortran stages.  Each host-pointer entry point below mirrors one Fortran
+ * subroutine: same argument meaning, same array layouts (Fortran
+ * column-major, 1-based index semantics inside the tables, the state index
+ * first/fastest, except ro4(W,n,n,n,n,M) whose state index is last), and the
+ * same in/out behaviour (the one-electron scratch f(*) is overwritten with the
+ * builder's own operator on the active upper triangle, exactly as the
+ * reference does).  Integer arguments are int64_t because the reference is
+ * built with -fdefault-integer-8 (CMakeLists.txt:18, cmake/FortranFlags.cmake:16-20).
+ *
+ * The Fortran drivers keep allocating every array; the library copies the
+ * inputs to the GPU, computes there, and copies the outputs back.  Every call
+ * returns an int status (NVPT_OK == 0); where the reference would `stop`, the
+ * library returns a nonzero status and nvpt_last_error() describes it.  The
+ * `_d` variants take device pointers and a CUDA stream (NULL = the context's
+ * stream) for callers that keep the tensors resident on the GPU; they enqueue
+ * work and return without synchronising.
+ *
+ * One context per host thread at a time; contexts are independent.
+ */
+#ifndef NVPT2_H
+#define NVPT2_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NVPT_OK 0
+#define NVPT_EINVAL 1    /* bad size or argument (reference: stop)        */
+#define NVPT_ECUDA 2     /* CUDA runtime / launch error                    */
+#define NVPT_ENOMEM 3    /* device allocation failed                       */
+#define NVPT_ENOTSUP 4   /* configuration outside the supported path       */
+#define NVPT_ETIMEDOUT 5 /* a bounded device-side wait gave up             */
+
+typedef struct nvpt_context nvpt_context;
+
+/* Context life cycle.  `device` is the CUDA ordinal. */
+int nvpt_create(nvpt_context **ctx, int device);
+int nvpt_destroy(nvpt_context *ctx);
+int nvpt_synchronize(nvpt_context *ctx);
+const char *nvpt_last_error(const nvpt_context *ctx);
+const char *nvpt_status_string(int status);
+/* Number of kernels this context has launched since creation. */
+int64_t nvpt_launch_count(const nvpt_context *ctx);
+
+/* ------------------------------------------------------------------ */
+/* Packed-index maps (integer, bit-exact).                             */
+/* ------------------------------------------------------------------ */
+
+/* src/indices_norm.F90:53 nwords = n(n+1)(n+2)(n+3)/24 */
+int64_t nvpt_nwords(int64_t nact);
+
+/* src/ord_utils.F90:71 ord8, applied on the device to `count` 8-tuples
+ * (1-based, row of 8 per tuple); out8 receives (i1..i8) per tuple and
+ * lindex receives lindice(i1,i2,i3,i4) (src/indices_norm.F90:64). */
+int nvpt_ord8(nvpt_context *ctx, int64_t nact, int64_t count, const int64_t *in8, int64_t *out8, int64_t *lindex);
+
+/* ------------------------------------------------------------------ */
+/* Stage 1 (koopro4QD.x): RDM partial traces, integrals, Koopmans.     */
+/* ------------------------------------------------------------------ */
+
+/* src/koopro4QD.F90:4881 bro3(ro4,daaa,nact,nele,metat):
+ * daaa(s,i,j,k,ii,jj,kk) = sum_l ro4[ord8(i,j,k,l;ii,jj,kk,l)] / (nele-3).
+ * daaa is overwritten (the reference driver zeroes it before the call). */
+int nvpt_bro3(nvpt_context *ctx, const double *ro4, double *daaa, int64_t nact, int64_t nele, int64_t metat);
+/* src/koopro4QD.F90:4961 bro2(daaa,taa,nact,nele,metat) */
+int nvpt_bro2(nvpt_context *ctx, const double *daaa, double *taa, int64_t nact, int64_t nele, int64_t metat);
+/* src/koopro4QD.F90:5002 bro1(taa,dal,nact,nele,metat) */
+int nvpt_bro1(nvpt_context *ctx, const double *taa, double *dal, int64_t nact, int64_t nele, int64_t metat);
+
+/* src/koopro4QD.F90:3900 get_aj_atwo(atwo,nact,ncore,norb,aj) on the
+ * Cholesky/DF integral path (src/ijkl_utils.F90:637 ai_cholesky).  The
+ * reference reads the integrals from module state; here they are passed:
+ * oneint(norb(norb+1)/2) and cholesky_array(nchovec, norb(norb+1)/2). */
+int nvpt_get_aj_atwo(nvpt_context *ctx, double *atwo, int64_t nact, int64_t ncore, int64_t norb, double *aj,
+                     const double *oneint, const double *cholesky_array, int64_t nchovec);
+
+/* src/koop_matrices.F90:16 koop_matrices_ctl(metat,nact,ncore,atwo,daaa,taa,dal,f,aj).
+ * The reference writes its results to nevpt.h5; they are returned here in
+ * the dataset shapes: ipko1/eako1 (metat,n,n) "1-IPKO"/"1-EAKO";
+ * hrdm2 (metat,n^4) "2-HRDM"; ipko2/eako2 (metat,n^4) "2-IPKO"/"2-EAKO";
+ * gk0pa/gk0pd (metat,n^4); gk0pf (metat,n,n).  f is in/out scratch of at
+ * least (ncore+nact)(ncore+nact+1)/2 elements. */
+int nvpt_koop_matrices_ctl(nvpt_context *ctx, int64_t metat, int64_t nact, int64_t ncore, const double *atwo,
+                           const double *daaa, const double *taa, const double *dal, double *f, const double *aj,
+                           double *ipko1, double *eako1, double *hrdm2, double *ipko2, double *eako2, double *gk0pa,
+                           double *gk0pd, double *gk0pf);
+
+/* src/koopro4QD.F90:3974 bamat(amat,atmat,atwo,ro4,daaa,taa,dal,nact,ncore,f,aj,norb,metat,nsym):
+ * amat "amatIP", atmat "amatEA", both (metat,n^6).  nsym must be 1. */
+int nvpt_bamat(nvpt_context *ctx, double *amat, double *atmat, const double *atwo, const double *ro4,
+               const double *daaa, const double *taa, const double *dal, int64_t nact, int64_t ncore, double *f,
+               const double *aj, int64_t norb, int64_t metat, int64_t nsym);
+
+/* src/koopro4QD.F90:4231 bbmat(atwo,bmat,btmat,daaa,taa,dal,nact,ncore,f,aj,metat) */
+int nvpt_bbmat(nvpt_context *ctx, const double *atwo, double *bmat, double *btmat, const double *daaa,
+               const double *taa, const double *dal, int64_t nact, int64_t ncore, double *f, const double *aj,
+               int64_t metat);
+/* src/koopro4QD.F90:4301 bcmat(atwo,cmat,ctmat,daaa,taa,dal,nact,ncore,f,aj,metat) */
+int nvpt_bcmat(nvpt_context *ctx, const double *atwo, double *cmat, double *ctmat, const double *daaa,
+               const double *taa, const double *dal, int64_t nact, int64_t ncore, double *f, const double *aj,
+               int64_t metat);
+/* src/koopro4QD.F90:4399 bdmat(atwo,dmat,dtmat,taa,dal,nact,ncore,f,aj,metat) */
+int nvpt_bdmat(nvpt_context *ctx, const double *atwo, double *dmat, double *dtmat, const double *taa,
+               const double *dal, int64_t nact, int64_t ncore, double *f, const double *aj, int64_t metat);
+
+/* ------------------------------------------------------------------ */
+/* Device-pointer variants (resident tensors, asynchronous).           */
+/* ------------------------------------------------------------------ */
+int nvpt_bro3_d(nvpt_context *ctx, const double *ro4, double *daaa, int64_t nact, int64_t nele, int64_t metat,
+                void *stream);
+int nvpt_bro2_d(nvpt_context *ctx, const double *daaa, double *taa, int64_t nact, int64_t nele, int64_t metat,
+                void *stream);
+int nvpt_bro1_d(nvpt_context *ctx, const double *taa, double *dal, int64_t nact, int64_t nele, int64_t metat,
+                void *stream);
+int nvpt_get_aj_atwo_d(nvpt_context *ctx, double *atwo, int64_t nact, int64_t ncore, int64_t norb, double *aj,
+                       const double *oneint, const double *cholesky_array, int64_t nchovec, void *stream);
+int nvpt_koop_matrices_ctl_d(nvpt_context *ctx, int64_t metat, int64_t nact, int64_t ncore, const double *atwo,
+                             const double *daaa, const double *taa, const double *dal, double *f, const double *aj,
+                             double *ipko1, double *eako1, double *hrdm2, double *ipko2, double *eako2,
+                             double *gk0pa, double *gk0pd, double *gk0pf, void *stream);
+int nvpt_bamat_d(nvpt_context *ctx, double *amat, double *atmat, const double *atwo, const double *ro4,
+                 const double *daaa, const double *taa, const double *dal, int64_t nact, int64_t ncore, double *f,
+                 const double *aj, int64_t norb, int64_t metat, int64_t nsym, void *stream);
+int nvpt_bbmat_d(nvpt_context *ctx, const double *atwo, double *bmat, double *btmat, const double *daaa,
+                 const double *taa, const double *dal, int64_t nact, int64_t ncore, double *f, const double *aj,
+                 int64_t metat, void *stream);
+int nvpt_bcmat_d(nvpt_context *ctx, const double *atwo, double *cmat, double *ctmat, const double *daaa,
+                 const double *taa, const double *dal, int64_t nact, int64_t ncore, double *f, const double *aj,
+                 int64_t metat, void *stream);
+int nvpt_bdmat_d(nvpt_context *ctx, const double *atwo, double *dmat, double *dtmat, const double *taa,
+                 const double *dal, int64_t nact, int64_t ncore, double *f, const double *aj, int64_t metat,
+                 void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NVPT2_H */

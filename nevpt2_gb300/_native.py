@@ -1,0 +1,130 @@
+"""Loader for the in-tree CUDA library ``libnvpt2.so`` (C ABI in include/nvpt2.h).
+
+There is no CPU fallback: if the library is missing or no GPU is visible the
+calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import re
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libnvpt2.so"
+HEADER = PKG.parent / "include" / "nvpt2.h"
+
+I64 = ctypes.c_int64
+P = ctypes.c_void_p
+
+_lib = None
+
+
+class NvptError(RuntimeError):
+    def __init__(self, status: int, what: str, detail: str):
+        super().__init__(f"{what} failed with status {status} ({STATUS.get(status, '?')}): {detail}")
+        self.status = status
+
+
+STATUS = {0: "NVPT_OK", 1: "NVPT_EINVAL", 2: "NVPT_ECUDA", 3: "NVPT_ENOMEM", 4: "NVPT_ENOTSUP", 5: "NVPT_ETIMEDOUT"}
+
+
+def header_functions() -> list[str]:
+    """Every function name include/nvpt2.h declares."""
+    txt = HEADER.read_text()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(nvpt_\w+)\s*\(", txt)))
+
+
+_SIGS = {
+    "nvpt_create": ([ctypes.POINTER(P), ctypes.c_int], ctypes.c_int),
+    "nvpt_destroy": ([P], ctypes.c_int),
+    "nvpt_synchronize": ([P], ctypes.c_int),
+    "nvpt_last_error": ([P], ctypes.c_char_p),
+    "nvpt_status_string": ([ctypes.c_int], ctypes.c_char_p),
+    "nvpt_launch_count": ([P], I64),
+    "nvpt_nwords": ([I64], I64),
+    "nvpt_ord8": ([P, I64, I64, P, P, P], ctypes.c_int),
+    "nvpt_bro3": ([P, P, P, I64, I64, I64], ctypes.c_int),
+    "nvpt_bro2": ([P, P, P, I64, I64, I64], ctypes.c_int),
+    "nvpt_bro1": ([P, P, P, I64, I64, I64], ctypes.c_int),
+    "nvpt_get_aj_atwo": ([P, P, I64, I64, I64, P, P, P, I64], ctypes.c_int),
+    "nvpt_koop_matrices_ctl": ([P, I64, I64, I64] + [P] * 15, ctypes.c_int),
+    "nvpt_bamat": ([P] + [P] * 7 + [I64, I64, P, P, I64, I64, I64], ctypes.c_int),
+    "nvpt_bbmat": ([P] + [P] * 6 + [I64, I64, P, P, I64], ctypes.c_int),
+    "nvpt_bcmat": ([P] + [P] * 6 + [I64, I64, P, P, I64], ctypes.c_int),
+    "nvpt_bdmat": ([P] + [P] * 5 + [I64, I64, P, P, I64], ctypes.c_int),
+    "nvpt_bro3_d": ([P, P, P, I64, I64, I64, P], ctypes.c_int),
+    "nvpt_bro2_d": ([P, P, P, I64, I64, I64, P], ctypes.c_int),
+    "nvpt_bro1_d": ([P, P, P, I64, I64, I64, P], ctypes.c_int),
+    "nvpt_get_aj_atwo_d": ([P, P, I64, I64, I64, P, P, P, I64, P], ctypes.c_int),
+    "nvpt_koop_matrices_ctl_d": ([P, I64, I64, I64] + [P] * 15 + [P], ctypes.c_int),
+    "nvpt_bamat_d": ([P] + [P] * 7 + [I64, I64, P, P, I64, I64, I64, P], ctypes.c_int),
+    "nvpt_bbmat_d": ([P] + [P] * 6 + [I64, I64, P, P, I64, P], ctypes.c_int),
+    "nvpt_bcmat_d": ([P] + [P] * 6 + [I64, I64, P, P, I64, P], ctypes.c_int),
+    "nvpt_bdmat_d": ([P] + [P] * 5 + [I64, I64, P, P, I64, P], ctypes.c_int),
+}
+
+
+def lib():
+    """Load libnvpt2.so (building it if the tree has no copy yet)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            from . import build
+            build.build_cuda()
+        L = ctypes.CDLL(str(LIB_PATH))
+        for name, (args, res) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+    return _lib
+
+
+def ptr(a) -> P | None:
+    """Address of a numpy array or a torch tensor (host or device)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return P(a.ctypes.data)
+    return P(a.data_ptr())
+
+
+class Context:
+    """Owns one nvpt_context (a CUDA device and stream)."""
+
+    def __init__(self, device: int = 0):
+        self._lib = lib()
+        h = P()
+        st = self._lib.nvpt_create(ctypes.byref(h), device)
+        if st != 0:
+            raise NvptError(st, "nvpt_create", "no usable CUDA device (the library has no CPU fallback)")
+        self.handle = h
+
+    def check(self, status: int, what: str) -> None:
+        if status != 0:
+            detail = self._lib.nvpt_last_error(self.handle)
+            raise NvptError(status, what, detail.decode() if detail else "")
+
+    def call(self, name: str, *args) -> None:
+        self.check(getattr(self._lib, name)(self.handle, *args), name)
+
+    def synchronize(self) -> None:
+        self.call("nvpt_synchronize")
+
+    @property
+    def launches(self) -> int:
+        return int(self._lib.nvpt_launch_count(self.handle))
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self._lib.nvpt_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,94 @@
+"""Build recipe for the in-tree native libraries.
+
+* ``libnvpt2.so``  - the CUDA library behind include/nvpt2.h, sm_103a only.
+* ``librdmgen.so`` - host (OpenMP) generator of exact RDMs for synthetic inputs.
+
+Both land next to this file so that the Python layer loads them from the
+source tree.  ``nvcc`` cross-compiles for sm_103a without a GPU.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+CSRC = PKG / "csrc"
+INCLUDE = PKG.parent / "include"
+GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
+
+CUDA_SOURCES = ["capi.cu", "koop_kernels.cu", "bamat.cu"]
+CUDA_HEADERS = ["eexx.cuh", "nvpt2_internal.h"]
+
+
+def _nvcc() -> str:
+    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not Path(cand).exists():
+        raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libnvpt2.so")
+    return cand
+
+
+def _stale(target: Path, deps: list[Path]) -> bool:
+    if not target.exists():
+        return True
+    t = target.stat().st_mtime
+    return any(d.stat().st_mtime > t for d in deps)
+
+
+def build_cuda(force: bool = False, verbose: bool = False) -> Path:
+    out = PKG / "libnvpt2.so"
+    deps = [CSRC / s for s in CUDA_SOURCES + CUDA_HEADERS] + [INCLUDE / "nvpt2.h"]
+    if not force and not _stale(out, deps):
+        return out
+    objdir = PKG / "_build"
+    objdir.mkdir(exist_ok=True)
+    nvcc = _nvcc()
+    flags = [GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+             f"-I{INCLUDE}", f"-I{CSRC}"]
+    procs = []
+    objs = []
+    for src in CUDA_SOURCES:
+        obj = objdir / (Path(src).stem + ".o")
+        objs.append(obj)
+        cmd = [nvcc, *flags, "-c", str(CSRC / src), "-o", str(obj)]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
+    for cmd, p in procs:
+        txt, _ = p.communicate()
+        if p.returncode != 0:
+            raise RuntimeError(f"nvcc failed ({' '.join(cmd)}):\n{txt}")
+        if verbose and txt:
+            print(txt)
+    tmp = out.with_suffix(".so.tmp")
+    cmd = [nvcc, GENCODE, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed: {r.stdout}\n{r.stderr}")
+    os.replace(tmp, out)
+    return out
+
+
+def build_rdmgen(force: bool = False) -> Path:
+    out = PKG / "librdmgen.so"
+    src = CSRC / "rdmgen.cpp"
+    if not force and not _stale(out, [src]):
+        return out
+    tmp = out.with_suffix(".so.tmp")
+    cmd = ["g++", "-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared", str(src), "-o", str(tmp)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"g++ failed: {r.stdout}\n{r.stderr}")
+    os.replace(tmp, out)
+    return out
+
+
+def build_all(force: bool = False, verbose: bool = False) -> None:
+    build_rdmgen(force)
+    build_cuda(force, verbose)
+
+
+if __name__ == "__main__":
+    build_all(force="--force" in sys.argv, verbose="-v" in sys.argv)

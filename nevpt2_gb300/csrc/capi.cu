@@ -1,0 +1,447 @@
+// C ABI of the library (include/nvpt2.h): context handling, argument checks,
+// host<->device staging for the drop-in host-pointer entry points, and the
+// device-pointer (_d) entry points that enqueue the kernels.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/nvpt2.h"
+#include "nvpt2_internal.h"
+
+namespace nvpt {
+std::atomic<long long> g_launches{0};
+
+// src/ord_utils.F90:71 ord8 over a batch of tuples (bit-exactness tests).
+__global__ void k_ord8(const int64_t *in8, int64_t *out8, int64_t *lindex, long long count) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const int64_t *x = in8 + 8 * t;
+    int q0, q1, q2, q3;
+    int a1 = (int)x[0], c1 = (int)x[1], e1 = (int)x[2], g1 = (int)x[3];
+    int a2 = (int)x[4], c2 = (int)x[5], e2 = (int)x[6], g2 = (int)x[7];
+    int ind = ord8_key(a1, c1, e1, g1, a2, c2, e2, g2, q0, q1, q2, q3);
+    // recover the sorted key from the packed index: the key group is the one
+    // with the larger normind (first on ties), sorted descending
+    int k[4];
+    if (normind4(a1, c1, e1, g1) >= normind4(a2, c2, e2, g2)) { k[0] = a1; k[1] = c1; k[2] = e1; k[3] = g1; }
+    else { k[0] = a2; k[1] = c2; k[2] = e2; k[3] = g2; }
+    for (int i = 0; i < 4; ++i)
+        for (int j = i + 1; j < 4; ++j)
+            if (k[j] > k[i]) { int tt = k[i]; k[i] = k[j]; k[j] = tt; }
+    out8[8 * t + 0] = k[0]; out8[8 * t + 1] = k[1]; out8[8 * t + 2] = k[2]; out8[8 * t + 3] = k[3];
+    out8[8 * t + 4] = q0; out8[8 * t + 5] = q1; out8[8 * t + 6] = q2; out8[8 * t + 7] = q3;
+    lindex[t] = ind;
+}
+
+void launch_ord8(const int64_t *in8, int64_t *out8, int64_t *lindex, long long count, cudaStream_t st) {
+    k_ord8<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(in8, out8, lindex, count);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+}  // namespace nvpt
+
+using namespace nvpt;
+
+struct nvpt_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    long long launches_at_create = 0;
+};
+
+namespace {
+
+const int64_t kMaxNact = 16;  // packed-index arithmetic and generator limits
+
+int fail(nvpt_context *ctx, int code, const std::string &msg) {
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+int cuda_check(nvpt_context *ctx, cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return NVPT_OK;
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    return fail(ctx, e == cudaErrorMemoryAllocation ? NVPT_ENOMEM : NVPT_ECUDA, m);
+}
+
+#define NV_TRY(expr)                 \
+    do {                             \
+        int _st = (expr);            \
+        if (_st != NVPT_OK) return _st; \
+    } while (0)
+
+cudaStream_t pick(nvpt_context *ctx, void *stream) { return stream ? (cudaStream_t)stream : ctx->stream; }
+
+int check_nact(nvpt_context *ctx, int64_t nact, int64_t metat) {
+    if (!ctx) return NVPT_EINVAL;
+    if (nact < 1 || nact > kMaxNact) return fail(ctx, NVPT_EINVAL, "nact must be in [1,16]");
+    if (metat < 1 || metat > 64) return fail(ctx, NVPT_EINVAL, "metat must be in [1,64]");
+    return NVPT_OK;
+}
+
+int after_launch(nvpt_context *ctx, const char *what) { return cuda_check(ctx, cudaGetLastError(), what); }
+
+Rdm make_rdm(int64_t n, int64_t M, const double *d1, const double *d2, const double *d3, const double *ro4) {
+    Rdm r;
+    r.n = (int)n;
+    r.M = (int)M;
+    r.W = n * (n + 1) * (n + 2) * (n + 3) / 24;
+    r.d1 = d1; r.d2 = d2; r.d3 = d3; r.ro4 = ro4;
+    return r;
+}
+
+int64_t ipow(int64_t b, int e) {
+    int64_t r = 1;
+    for (int i = 0; i < e; ++i) r *= b;
+    return r;
+}
+
+int64_t f_len(int64_t nact, int64_t ncore) { return (ncore + nact) * (ncore + nact + 1) / 2; }
+
+// Stream-ordered device staging area for one host-pointer call.
+struct Stage {
+    nvpt_context *ctx;
+    cudaStream_t st;
+    std::vector<void *> bufs;
+    int status = NVPT_OK;
+    Stage(nvpt_context *c) : ctx(c), st(c->stream) {}
+    ~Stage() {
+        for (void *p : bufs) cudaFreeAsync(p, st);
+        cudaStreamSynchronize(st);
+    }
+    double *alloc(int64_t count) {
+        if (status != NVPT_OK) return nullptr;
+        void *p = nullptr;
+        cudaError_t e = cudaMallocAsync(&p, sizeof(double) * (size_t)(count > 0 ? count : 1), st);
+        if (e != cudaSuccess) { status = cuda_check(ctx, e, "cudaMallocAsync"); return nullptr; }
+        bufs.push_back(p);
+        return (double *)p;
+    }
+    double *up(const double *h, int64_t count) {
+        double *d = alloc(count);
+        if (!d) return nullptr;
+        cudaError_t e = cudaMemcpyAsync(d, h, sizeof(double) * (size_t)count, cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) { status = cuda_check(ctx, e, "H2D copy"); return nullptr; }
+        return d;
+    }
+    int down(double *h, const double *d, int64_t count) {
+        if (status != NVPT_OK) return status;
+        cudaError_t e = cudaMemcpyAsync(h, d, sizeof(double) * (size_t)count, cudaMemcpyDeviceToHost, st);
+        if (e != cudaSuccess) status = cuda_check(ctx, e, "D2H copy");
+        return status;
+    }
+    int finish() {
+        if (status != NVPT_OK) return status;
+        return cuda_check(ctx, cudaStreamSynchronize(st), "stream synchronize");
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+int nvpt_create(nvpt_context **out, int device) {
+    if (!out) return NVPT_EINVAL;
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) return NVPT_ECUDA;
+    if (device < 0 || device >= ndev) return NVPT_EINVAL;
+    nvpt_context *ctx = new nvpt_context();
+    ctx->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete ctx;
+        return NVPT_ECUDA;
+    }
+    ctx->launches_at_create = g_launches.load();
+    *out = ctx;
+    return NVPT_OK;
+}
+
+int nvpt_destroy(nvpt_context *ctx) {
+    if (!ctx) return NVPT_EINVAL;
+    cudaStreamSynchronize(ctx->stream);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return NVPT_OK;
+}
+
+int nvpt_synchronize(nvpt_context *ctx) {
+    if (!ctx) return NVPT_EINVAL;
+    return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "stream synchronize");
+}
+
+const char *nvpt_last_error(const nvpt_context *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+const char *nvpt_status_string(int status) {
+    switch (status) {
+        case NVPT_OK: return "ok";
+        case NVPT_EINVAL: return "invalid argument";
+        case NVPT_ECUDA: return "CUDA error";
+        case NVPT_ENOMEM: return "device allocation failed";
+        case NVPT_ENOTSUP: return "unsupported configuration";
+        case NVPT_ETIMEDOUT: return "device wait timed out";
+        default: return "unknown status";
+    }
+}
+
+int64_t nvpt_launch_count(const nvpt_context *ctx) { return ctx ? g_launches.load() - ctx->launches_at_create : 0; }
+
+int64_t nvpt_nwords(int64_t nact) { return nact * (nact + 1) * (nact + 2) * (nact + 3) / 24; }
+
+int nvpt_ord8(nvpt_context *ctx, int64_t nact, int64_t count, const int64_t *in8, int64_t *out8, int64_t *lindex) {
+    NV_TRY(check_nact(ctx, nact, 1));
+    if (count < 0 || (count > 0 && (!in8 || !out8 || !lindex))) return fail(ctx, NVPT_EINVAL, "ord8: bad buffers");
+    for (int64_t i = 0; i < 8 * count; ++i)
+        if (in8[i] < 1 || in8[i] > nact) return fail(ctx, NVPT_EINVAL, "ord8: index outside [1,nact]");
+    if (count == 0) return NVPT_OK;
+    cudaStream_t st = ctx->stream;
+    int64_t *d = nullptr;
+    size_t bytes = sizeof(int64_t) * (size_t)count * 17;
+    NV_TRY(cuda_check(ctx, cudaMallocAsync((void **)&d, bytes, st), "cudaMallocAsync"));
+    cudaMemcpyAsync(d, in8, sizeof(int64_t) * 8 * count, cudaMemcpyHostToDevice, st);
+    launch_ord8(d, d + 8 * count, d + 16 * count, count, st);
+    int rc = after_launch(ctx, "ord8 launch");
+    cudaMemcpyAsync(out8, d + 8 * count, sizeof(int64_t) * 8 * count, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(lindex, d + 16 * count, sizeof(int64_t) * count, cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(d, st);
+    int rc2 = cuda_check(ctx, cudaStreamSynchronize(st), "ord8 sync");
+    return rc != NVPT_OK ? rc : rc2;
+}
+
+// ----------------------------------------------------------------- _d entries
+int nvpt_bro3_d(nvpt_context *ctx, const double *ro4, double *daaa, int64_t nact, int64_t nele, int64_t metat,
+                void *stream) {
+    NV_TRY(check_nact(ctx, nact, metat));
+    if (nele <= 3) return fail(ctx, NVPT_EINVAL, "bro3 needs nele > 3 (it divides by nele-3)");
+    Rdm r = make_rdm(nact, metat, nullptr, nullptr, nullptr, ro4);
+    launch_bro3(r, daaa, (int)nele, pick(ctx, stream));
+    return after_launch(ctx, "bro3");
+}
+
+int nvpt_bro2_d(nvpt_context *ctx, const double *daaa, double *taa, int64_t nact, int64_t nele, int64_t metat,
+                void *stream) {
+    NV_TRY(check_nact(ctx, nact, metat));
+    if (nele <= 2) return fail(ctx, NVPT_EINVAL, "bro2 needs nele > 2");
+    Rdm r = make_rdm(nact, metat, nullptr, nullptr, daaa, nullptr);
+    launch_bro2(r, taa, (int)nele, pick(ctx, stream));
+    return after_launch(ctx, "bro2");
+}
+
+int nvpt_bro1_d(nvpt_context *ctx, const double *taa, double *dal, int64_t nact, int64_t nele, int64_t metat,
+                void *stream) {
+    NV_TRY(check_nact(ctx, nact, metat));
+    if (nele <= 1) return fail(ctx, NVPT_EINVAL, "bro1 needs nele > 1");
+    Rdm r = make_rdm(nact, metat, nullptr, taa, nullptr, nullptr);
+    launch_bro1(r, dal, (int)nele, pick(ctx, stream));
+    return after_launch(ctx, "bro1");
+}
+
+int nvpt_get_aj_atwo_d(nvpt_context *ctx, double *atwo, int64_t nact, int64_t ncore, int64_t norb, double *aj,
+                       const double *oneint, const double *chol, int64_t nchovec, void *stream) {
+    NV_TRY(check_nact(ctx, nact, 1));
+    if (ncore < 0 || norb < ncore + nact || nchovec < 1) return fail(ctx, NVPT_EINVAL, "get_aj_atwo: bad sizes");
+    launch_aj_atwo(oneint, chol, (int)nchovec, (int)nact, (int)ncore, (int)norb, atwo, aj, pick(ctx, stream));
+    return after_launch(ctx, "get_aj_atwo");
+}
+
+int nvpt_koop_matrices_ctl_d(nvpt_context *ctx, int64_t metat, int64_t nact, int64_t ncore, const double *atwo,
+                             const double *daaa, const double *taa, const double *dal, double *f, const double *aj,
+                             double *ipko1, double *eako1, double *hrdm2, double *ipko2, double *eako2,
+                             double *gk0pa, double *gk0pd, double *gk0pf, void *stream) {
+    NV_TRY(check_nact(ctx, nact, metat));
+    if (ncore < 0) return fail(ctx, NVPT_EINVAL, "koop_matrices_ctl: ncore < 0");
+    cudaStream_t st = pick(ctx, stream);
+    Rdm r = make_rdm(nact, metat, dal, taa, daaa, nullptr);
+    int n = (int)nact, nc = (int)ncore;
+    launch_build_f(f, aj, atwo, n, nc, 0, st);
+    launch_koopE(r, atwo, f, nc, ipko1, eako1, st);
+    launch_hrdm(r, hrdm2, st);
+    launch_build_f(f, aj, atwo, n, nc, 1, st);
+    launch_koop2E(r, atwo, f, nc, ipko2, eako2, st);
+    launch_koop0p(r, atwo, f, nc, gk0pa, gk0pd, gk0pf, st);
+    return after_launch(ctx, "koop_matrices_ctl");
+}
+
+int nvpt_bamat_d(nvpt_context *ctx, double *amat, double *atmat, const double *atwo, const double *ro4,
+                 const double *daaa, const double *taa, const double *dal, int64_t nact, int64_t ncore, double *f,
+                 const double *aj, int64_t norb, int64_t metat, int64_t nsym, void *stream) {
+    NV_TRY(check_nact(ctx, nact, metat));
+    if (nsym != 1) return fail(ctx, NVPT_ENOTSUP, "bamat: only the C1 (nsym=1) path is implemented");
+    if (norb < ncore + nact) return fail(ctx, NVPT_EINVAL, "bamat: norb < ncore+nact");
+    cudaStream_t st = pick(ctx, stream);
+    Rdm r = make_rdm(nact, metat, dal, taa, daaa, ro4);
+    launch_build_f(f, aj, atwo, (int)nact, (int)ncore, 1, st);
+    launch_bamat_direct(r, atwo, f, (int)ncore, amat, atmat, st);
+    return after_launch(ctx, "bamat");
+}
+
+int nvpt_bbmat_d(nvpt_context *ctx, const double *atwo, double *bmat, double *btmat, const double *daaa,
+                 const double *taa, const double *dal, int64_t nact, int64_t ncore, double *f, const double *aj,
+                 int64_t metat, void *stream) {
+    NV_TRY(check_nact(ctx, nact, metat));
+    cudaStream_t st = pick(ctx, stream);
+    Rdm r = make_rdm(nact, metat, dal, taa, daaa, nullptr);
+    launch_build_f(f, aj, atwo, (int)nact, (int)ncore, 2, st);
+    launch_bbmat(r, atwo, f, aj, (int)ncore, bmat, btmat, st);
+    return after_launch(ctx, "bbmat");
+}
+
+int nvpt_bcmat_d(nvpt_context *ctx, const double *atwo, double *cmat, double *ctmat, const double *daaa,
+                 const double *taa, const double *dal, int64_t nact, int64_t ncore, double *f, const double *aj,
+                 int64_t metat, void *stream) {
+    NV_TRY(check_nact(ctx, nact, metat));
+    cudaStream_t st = pick(ctx, stream);
+    Rdm r = make_rdm(nact, metat, dal, taa, daaa, nullptr);
+    launch_build_f(f, aj, atwo, (int)nact, (int)ncore, 1, st);
+    launch_bcmat(r, atwo, f, (int)ncore, cmat, ctmat, st);
+    return after_launch(ctx, "bcmat");
+}
+
+int nvpt_bdmat_d(nvpt_context *ctx, const double *atwo, double *dmat, double *dtmat, const double *taa,
+                 const double *dal, int64_t nact, int64_t ncore, double *f, const double *aj, int64_t metat,
+                 void *stream) {
+    NV_TRY(check_nact(ctx, nact, metat));
+    cudaStream_t st = pick(ctx, stream);
+    Rdm r = make_rdm(nact, metat, dal, taa, nullptr, nullptr);
+    launch_build_f(f, aj, atwo, (int)nact, (int)ncore, 2, st);
+    launch_bdmat(r, atwo, f, aj, (int)ncore, dmat, dtmat, st);
+    return after_launch(ctx, "bdmat");
+}
+
+// ----------------------------------------------------------- host entries
+int nvpt_bro3(nvpt_context *ctx, const double *ro4, double *daaa, int64_t nact, int64_t nele, int64_t metat) {
+    NV_TRY(check_nact(ctx, nact, metat));
+    int64_t W = nvpt_nwords(nact), n4 = ipow(nact, 4), n6 = ipow(nact, 6);
+    Stage S(ctx);
+    const double *d_ro4 = S.up(ro4, W * n4 * metat);
+    double *d_out = S.alloc(n6 * metat);
+    if (S.status) return S.status;
+    NV_TRY(nvpt_bro3_d(ctx, d_ro4, d_out, nact, nele, metat, nullptr));
+    S.down(daaa, d_out, n6 * metat);
+    return S.finish();
+}
+
+int nvpt_bro2(nvpt_context *ctx, const double *daaa, double *taa, int64_t nact, int64_t nele, int64_t metat) {
+    NV_TRY(check_nact(ctx, nact, metat));
+    int64_t n4 = ipow(nact, 4), n6 = ipow(nact, 6);
+    Stage S(ctx);
+    const double *d_in = S.up(daaa, n6 * metat);
+    double *d_out = S.alloc(n4 * metat);
+    if (S.status) return S.status;
+    NV_TRY(nvpt_bro2_d(ctx, d_in, d_out, nact, nele, metat, nullptr));
+    S.down(taa, d_out, n4 * metat);
+    return S.finish();
+}
+
+int nvpt_bro1(nvpt_context *ctx, const double *taa, double *dal, int64_t nact, int64_t nele, int64_t metat) {
+    NV_TRY(check_nact(ctx, nact, metat));
+    int64_t n2 = ipow(nact, 2), n4 = ipow(nact, 4);
+    Stage S(ctx);
+    const double *d_in = S.up(taa, n4 * metat);
+    double *d_out = S.alloc(n2 * metat);
+    if (S.status) return S.status;
+    NV_TRY(nvpt_bro1_d(ctx, d_in, d_out, nact, nele, metat, nullptr));
+    S.down(dal, d_out, n2 * metat);
+    return S.finish();
+}
+
+int nvpt_get_aj_atwo(nvpt_context *ctx, double *atwo, int64_t nact, int64_t ncore, int64_t norb, double *aj,
+                     const double *oneint, const double *chol, int64_t nchovec) {
+    NV_TRY(check_nact(ctx, nact, 1));
+    if (ncore < 0 || norb < ncore + nact || nchovec < 1) return fail(ctx, NVPT_EINVAL, "get_aj_atwo: bad sizes");
+    int64_t npair = norb * (norb + 1) / 2;
+    Stage S(ctx);
+    const double *d_one = S.up(oneint, npair);
+    const double *d_L = S.up(chol, npair * nchovec);
+    double *d_atwo = S.alloc(ipow(nact, 4));
+    double *d_aj = S.alloc(npair);
+    if (S.status) return S.status;
+    NV_TRY(nvpt_get_aj_atwo_d(ctx, d_atwo, nact, ncore, norb, d_aj, d_one, d_L, nchovec, nullptr));
+    S.down(atwo, d_atwo, ipow(nact, 4));
+    S.down(aj, d_aj, npair);
+    return S.finish();
+}
+
+int nvpt_koop_matrices_ctl(nvpt_context *ctx, int64_t metat, int64_t nact, int64_t ncore, const double *atwo,
+                           const double *daaa, const double *taa, const double *dal, double *f, const double *aj,
+                           double *ipko1, double *eako1, double *hrdm2, double *ipko2, double *eako2, double *gk0pa,
+                           double *gk0pd, double *gk0pf) {
+    NV_TRY(check_nact(ctx, nact, metat));
+    int64_t M = metat, n2 = ipow(nact, 2), n4 = ipow(nact, 4), n6 = ipow(nact, 6), nf = f_len(nact, ncore);
+    Stage S(ctx);
+    const double *d_atwo = S.up(atwo, n4);
+    const double *d3 = S.up(daaa, n6 * M), *d2 = S.up(taa, n4 * M), *d1 = S.up(dal, n2 * M);
+    double *d_f = S.up(f, nf);
+    const double *d_aj = S.up(aj, nf);
+    double *o_ip1 = S.alloc(n2 * M), *o_ea1 = S.alloc(n2 * M), *o_h = S.alloc(n4 * M), *o_ip2 = S.alloc(n4 * M);
+    double *o_ea2 = S.alloc(n4 * M), *o_a = S.alloc(n4 * M), *o_d = S.alloc(n4 * M), *o_f = S.alloc(n2 * M);
+    if (S.status) return S.status;
+    NV_TRY(nvpt_koop_matrices_ctl_d(ctx, metat, nact, ncore, d_atwo, d3, d2, d1, d_f, d_aj, o_ip1, o_ea1, o_h, o_ip2,
+                                    o_ea2, o_a, o_d, o_f, nullptr));
+    S.down(ipko1, o_ip1, n2 * M); S.down(eako1, o_ea1, n2 * M); S.down(hrdm2, o_h, n4 * M);
+    S.down(ipko2, o_ip2, n4 * M); S.down(eako2, o_ea2, n4 * M); S.down(gk0pa, o_a, n4 * M);
+    S.down(gk0pd, o_d, n4 * M); S.down(gk0pf, o_f, n2 * M); S.down(f, d_f, nf);
+    return S.finish();
+}
+
+int nvpt_bamat(nvpt_context *ctx, double *amat, double *atmat, const double *atwo, const double *ro4,
+               const double *daaa, const double *taa, const double *dal, int64_t nact, int64_t ncore, double *f,
+               const double *aj, int64_t norb, int64_t metat, int64_t nsym) {
+    NV_TRY(check_nact(ctx, nact, metat));
+    if (nsym != 1) return fail(ctx, NVPT_ENOTSUP, "bamat: only the C1 (nsym=1) path is implemented");
+    int64_t M = metat, n2 = ipow(nact, 2), n4 = ipow(nact, 4), n6 = ipow(nact, 6), nf = f_len(nact, ncore);
+    int64_t W = nvpt_nwords(nact);
+    Stage S(ctx);
+    const double *d_atwo = S.up(atwo, n4);
+    const double *d_ro4 = S.up(ro4, W * n4 * M);
+    const double *d3 = S.up(daaa, n6 * M), *d2 = S.up(taa, n4 * M), *d1 = S.up(dal, n2 * M);
+    double *d_f = S.up(f, nf);
+    const double *d_aj = S.up(aj, nf);
+    double *o_a = S.alloc(n6 * M), *o_at = S.alloc(n6 * M);
+    if (S.status) return S.status;
+    NV_TRY(nvpt_bamat_d(ctx, o_a, o_at, d_atwo, d_ro4, d3, d2, d1, nact, ncore, d_f, d_aj, norb, metat, nsym, nullptr));
+    S.down(amat, o_a, n6 * M); S.down(atmat, o_at, n6 * M); S.down(f, d_f, nf);
+    return S.finish();
+}
+
+static int bcd_host(nvpt_context *ctx, int which, const double *atwo, double *x, double *xt, const double *daaa,
+                    const double *taa, const double *dal, int64_t nact, int64_t ncore, double *f, const double *aj,
+                    int64_t metat) {
+    NV_TRY(check_nact(ctx, nact, metat));
+    int64_t M = metat, n2 = ipow(nact, 2), n4 = ipow(nact, 4), n6 = ipow(nact, 6), nf = f_len(nact, ncore);
+    int64_t nout = (which == 3 ? n2 : n4) * M;
+    Stage S(ctx);
+    const double *d_atwo = S.up(atwo, n4);
+    const double *d3 = which == 3 ? nullptr : S.up(daaa, n6 * M);
+    const double *d2 = S.up(taa, n4 * M), *d1 = S.up(dal, n2 * M);
+    double *d_f = S.up(f, nf);
+    const double *d_aj = S.up(aj, nf);
+    double *o = S.alloc(nout), *ot = S.alloc(nout);
+    if (S.status) return S.status;
+    int rc;
+    if (which == 1) rc = nvpt_bbmat_d(ctx, d_atwo, o, ot, d3, d2, d1, nact, ncore, d_f, d_aj, metat, nullptr);
+    else if (which == 2) rc = nvpt_bcmat_d(ctx, d_atwo, o, ot, d3, d2, d1, nact, ncore, d_f, d_aj, metat, nullptr);
+    else rc = nvpt_bdmat_d(ctx, d_atwo, o, ot, d2, d1, nact, ncore, d_f, d_aj, metat, nullptr);
+    if (rc != NVPT_OK) return rc;
+    S.down(x, o, nout); S.down(xt, ot, nout); S.down(f, d_f, nf);
+    return S.finish();
+}
+
+int nvpt_bbmat(nvpt_context *ctx, const double *atwo, double *bmat, double *btmat, const double *daaa,
+               const double *taa, const double *dal, int64_t nact, int64_t ncore, double *f, const double *aj,
+               int64_t metat) {
+    return bcd_host(ctx, 1, atwo, bmat, btmat, daaa, taa, dal, nact, ncore, f, aj, metat);
+}
+int nvpt_bcmat(nvpt_context *ctx, const double *atwo, double *cmat, double *ctmat, const double *daaa,
+               const double *taa, const double *dal, int64_t nact, int64_t ncore, double *f, const double *aj,
+               int64_t metat) {
+    return bcd_host(ctx, 2, atwo, cmat, ctmat, daaa, taa, dal, nact, ncore, f, aj, metat);
+}
+int nvpt_bdmat(nvpt_context *ctx, const double *atwo, double *dmat, double *dtmat, const double *taa,
+               const double *dal, int64_t nact, int64_t ncore, double *f, const double *aj, int64_t metat) {
+    return bcd_host(ctx, 3, atwo, dmat, dtmat, nullptr, taa, dal, nact, ncore, f, aj, metat);
+}
+
+}  // extern "C"

@@ -1,0 +1,467 @@
+// Stage-1 kernels: partial traces of the packed 4-RDM, active integrals and
+// the generalised Koopmans matrices, FP64.
+//
+// One thread owns one output element and performs the reference's reduction
+// for it in the reference's summation order, so no atomics are needed and
+// results are deterministic.  The reference loop nests each kernel restates
+// are cited on the kernel.  The n^9 A-matrix builder has its own file
+// (bamat.cu); this file holds the n^5..n^7 work.
+#include "nvpt2_internal.h"
+
+namespace nvpt {
+
+#define ATWO(i, j, k, l) atwo[((i)-1) + (ll)n * (((j)-1) + (ll)n * (((k)-1) + (ll)n * ((l)-1)))]
+#define FF(i, j) f[tri_index((i) + ncore, (j) + ncore) - 1]
+#define AJ(i, j) aj[tri_index((i) + ncore, (j) + ncore) - 1]
+#define O3(arr, s, a, b) arr[((s)-1) + (ll)M * (((a)-1) + (ll)n * ((b)-1))]
+#define O5(arr, s, a, b, c, d) arr[((s)-1) + (ll)M * (((a)-1) + (ll)n * (((b)-1) + (ll)n * (((c)-1) + (ll)n * ((d)-1))))]
+
+// Decode a flat 0-based index into `k` 1-based orbital indices, first fastest.
+__device__ __forceinline__ void decode(ll x, int n, int k, int *out) {
+    for (int i = 0; i < k; ++i) { out[i] = (int)(x % n) + 1; x /= n; }
+}
+
+// ---------------------------------------------------------------------------
+// One-electron operator of each builder (src/koop_matrices.F90:191-200 and
+// siblings): active upper triangle of f, mode 0: aj; 1: aj - 1/2 sum_c
+// atwo(a,c,c,b); 2: aj - sum_c atwo(a,c,c,b).
+__global__ void k_build_f(double *f, const double *aj, const double *atwo, int n, int ncore, int mode) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * n) return;
+    int a = t % n + 1, b = t / n + 1;
+    if (b < a) return;
+    double v = AJ(a, b);
+    if (mode != 0)
+        for (int c = 1; c <= n; ++c) v -= (mode == 1 ? 0.5 : 1.0) * ATWO(a, c, c, b);
+    FF(a, b) = v;
+}
+
+// ---------------------------------------------------------------------------
+// src/koopro4QD.F90:4881-4959 bro3.
+__global__ void k_bro3(Rdm r, double *daaa, double inv) {
+    const int n = r.n, M = r.M;
+    ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+    ll n6 = (ll)n * n * n * n * n * n;
+    if (t >= n6) return;
+    int x[6];
+    decode(t, n, 6, x);
+    const int i = x[0], j = x[1], k = x[2], ii = x[3], jj = x[4], kk = x[5];
+    for (int s = 1; s <= M; ++s) {
+        double acc = 0.0;
+        for (int l = 1; l <= n; ++l) {
+            int q0, q1, q2, q3;
+            int ind = ord8_key(i, j, k, l, ii, jj, kk, l, q0, q1, q2, q3);
+            acc += r.R4(ind, q0, q1, q2, q3, s);
+        }
+        daaa[(s - 1) + (ll)M * t] = acc * inv;
+    }
+}
+
+// src/koopro4QD.F90:4961-5000 bro2
+__global__ void k_bro2(Rdm r, double *taa, double inv) {
+    const int n = r.n, M = r.M;
+    ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (ll)n * n * n * n) return;
+    int x[4];
+    decode(t, n, 4, x);
+    for (int s = 1; s <= M; ++s) {
+        double acc = 0.0;
+        for (int l = 1; l <= n; ++l) acc += r.D3(s, x[0], x[1], l, x[2], x[3], l);
+        taa[(s - 1) + (ll)M * t] = acc * inv;
+    }
+}
+
+// src/koopro4QD.F90:5002-5049 bro1
+__global__ void k_bro1(Rdm r, double *dal, double inv) {
+    const int n = r.n, M = r.M;
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * n) return;
+    int i = t % n + 1, j = t / n + 1;
+    for (int s = 1; s <= M; ++s) {
+        double acc = 0.0;
+        for (int l = 1; l <= n; ++l) acc += r.D2(s, i, l, j, l);
+        dal[(s - 1) + (ll)M * t] = acc * inv;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// src/koopro4QD.F90:3900-3971 get_aj_atwo with the Cholesky integrals of
+// src/ijkl_utils.F90:637-688: (ij|kl) = sum_Q L(Q,indice(i,j)) L(Q,indice(k,l)).
+__device__ __forceinline__ double chol_ai(const double *L, int Q, int i, int j, int k, int l) {
+    const double *x = L + (ll)Q * (tri_index(i, j) - 1);
+    const double *y = L + (ll)Q * (tri_index(k, l) - 1);
+    double s = 0.0;
+    for (int q = 0; q < Q; ++q) s += x[q] * y[q];
+    return s;
+}
+
+__global__ void k_atwo(const double *L, int Q, int n, int ncore, double *atwo) {
+    ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (ll)n * n * n * n) return;
+    int x[4];
+    decode(t, n, 4, x);
+    atwo[t] = chol_ai(L, Q, x[0] + ncore, x[1] + ncore, x[2] + ncore, x[3] + ncore);
+}
+
+// aj(active upper triangle) = oneint + sum_{j<=ncore} [2(ab|jj) - (aj|jb)]; the
+// rest of aj is a copy of oneint (made by the caller).
+__global__ void k_aj(const double *oneint, const double *L, int Q, int n, int ncore, double *aj) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * n) return;
+    int a = t % n + 1, b = t / n + 1;
+    if (b < a) return;
+    int ac = a + ncore, bc = b + ncore;
+    ll jab = tri_index(ac, bc) - 1;
+    double v = oneint[jab];
+    for (int j = 1; j <= ncore; ++j) v = v + 2.0 * chol_ai(L, Q, ac, bc, j, j) - chol_ai(L, Q, ac, j, j, bc);
+    aj[jab] = v;
+}
+
+// ---------------------------------------------------------------------------
+// src/koop_matrices.F90:165-250 koopE.  Thread per (ap, a).
+__global__ void k_koopE(Rdm r, const double *atwo, const double *f, int ncore, double *koopipa, double *koopeaa) {
+    const int n = r.n, M = r.M;
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * n) return;
+    int ap = t % n + 1, a = t / n + 1;
+    for (int s = 1; s <= M; ++s) {
+        double ip = 0.0;
+        for (int c = 1; c <= n; ++c) {
+            ip -= FF(a, c) * r.D1(s, ap, c);
+            for (int d = 1; d <= n; ++d)
+                for (int ie = 1; ie <= n; ++ie) ip -= ATWO(c, ie, a, d) * r.D2(s, ap, c, d, ie);
+        }
+        ip = 2.0 * ip;
+        double dumm = 2.0 * FF(ap, a);
+        for (int d = 1; d <= n; ++d)
+            for (int ie = 1; ie <= n; ++ie) dumm += (2.0 * ATWO(d, ie, ap, a) - ATWO(ap, ie, d, a)) * r.D1(s, d, ie);
+        O3(koopipa, s, ap, a) = ip;
+        O3(koopeaa, s, ap, a) = ip + 2.0 * dumm;
+    }
+}
+
+// src/koop_matrices.F90:78-88 (2-HRDM through ro2t)
+__global__ void k_hrdm(Rdm r, double *hrdm) {
+    const int n = r.n, M = r.M;
+    ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (ll)n * n * n * n) return;
+    int x[4];
+    decode(t, n, 4, x);
+    for (int s = 1; s <= M; ++s) hrdm[(s - 1) + (ll)M * t] = r.ro2t(x[0], x[1], x[2], x[3], s);
+}
+
+// src/koop_matrices.F90:297-335 koop2E, 2-IP part.  Thread per (ap,bp,a,b).
+__global__ void k_koop2E_ip(Rdm r, const double *atwo, const double *f, int ncore, double *koopaa) {
+    const int n = r.n, M = r.M;
+    ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (ll)n * n * n * n) return;
+    int x[4];
+    decode(t, n, 4, x);
+    const int ap = x[0], bp = x[1], a = x[2], b = x[3];
+    for (int s = 1; s <= M; ++s) {
+        double acc = 0.0;
+        for (int d = 1; d <= n; ++d) {
+            acc = acc - FF(a, d) * r.D2(s, ap, bp, d, b) - FF(b, d) * r.D2(s, ap, bp, a, d);
+            for (int ie = 1; ie <= n; ++ie)
+                for (int ief = 1; ief <= n; ++ief) {
+                    double dint = ATWO(d, ie, a, ief), dint2 = ATWO(d, ie, b, ief);
+                    double dum = r.D3(s, ap, bp, d, ief, b, ie);
+                    if (d == ief) dum += 0.5 * r.D2(s, ap, bp, ie, b);
+                    if (d == b) dum += 0.5 * r.D2(s, ap, bp, ief, ie);
+                    acc -= dint * dum;
+                    dum = r.D3(s, ap, bp, d, a, ief, ie);
+                    if (d == a) dum += 0.5 * r.D2(s, ap, bp, ie, ief);
+                    if (d == ief) dum += 0.5 * r.D2(s, ap, bp, a, ie);
+                    acc -= dint2 * dum;
+                }
+        }
+        O5(koopaa, s, ap, bp, a, b) = acc;
+    }
+}
+
+// src/koop_matrices.F90:336-384 koop2E, 2-EA part.  Thread per (ap,bp,a,b).
+__global__ void k_koop2E_ea(Rdm r, const double *atwo, const double *f, int ncore, double *koopeaa) {
+    const int n = r.n, M = r.M;
+    ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (ll)n * n * n * n) return;
+    int x[4];
+    decode(t, n, 4, x);
+    const int ap = x[0], bp = x[1], a = x[2], b = x[3];
+    for (int s = 1; s <= M; ++s) {
+        double acc = 0.0;
+        for (int c = 1; c <= n; ++c) {
+            acc += FF(a, c) * r.ro2t(ap, bp, c, b, s) + FF(b, c) * r.ro2t(ap, bp, a, c, s);
+            for (int d = 1; d <= n; ++d)
+                for (int ie = 1; ie <= n; ++ie) {
+                    double dint = ATWO(c, ie, d, a);
+                    double dum = -r.ro3t(ap, bp, ie, d, b, c, s);
+                    if (c == ie) dum += 2.0 * r.ro2t(ap, bp, d, b, s);
+                    if (d == ie) dum -= 0.5 * r.ro2t(ap, bp, c, b, s);
+                    if (b == ie) dum -= 0.5 * r.ro2t(ap, bp, d, c, s);
+                    acc += dint * dum;
+                    dint = ATWO(c, ie, d, b);
+                    dum = -r.ro3t(ap, bp, ie, a, d, c, s);
+                    if (c == ie) dum += 2.0 * r.ro2t(ap, bp, a, d, s);
+                    if (a == ie) dum -= 0.5 * r.ro2t(ap, bp, c, d, s);
+                    if (d == ie) dum -= 0.5 * r.ro2t(ap, bp, a, c, s);
+                    acc += dint * dum;
+                }
+        }
+        O5(koopeaa, s, ap, bp, a, b) = acc;
+    }
+}
+
+// src/koop_matrices.F90:433-541 koopman0pE, A (koopaa) and D (koopbb) of the
+// 0' class.  Thread per (bp,ap,a,b).
+__global__ void k_koop0p_ad(Rdm r, const double *atwo, const double *f, int ncore, double *koopaa,
+                            double *koopbb) {
+    const int n = r.n, M = r.M;
+    ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (ll)n * n * n * n) return;
+    int x[4];
+    decode(t, n, 4, x);
+    const int bp = x[0], ap = x[1], a = x[2], b = x[3];
+    for (int s = 1; s <= M; ++s) {
+        double A = 0.0, Dm = 0.0;
+        for (int c = 1; c <= n; ++c) {
+            double fca = FF(c, a), fbc = FF(b, c);
+            A += 2.0 * (fca * r.ee2(bp, ap, c, b, s) - fbc * r.ee2(bp, ap, a, c, s));
+            for (int d = 1; d <= n; ++d)
+                for (int ie = 1; ie <= n; ++ie) {
+                    double dum1 = r.eee2(bp, ap, c, ie, d, b, s) + r.eee2(bp, ap, d, b, c, ie, s);
+                    double dum2 = r.eee2(bp, ap, a, ie, c, d, s) + r.eee2(bp, ap, c, d, a, ie, s);
+                    A += ATWO(c, ie, d, a) * dum1 - ATWO(b, ie, c, d) * dum2;
+                }
+        }
+        for (int c = 1; c <= n; ++c) {
+            double fca = FF(c, a), fbc = FF(b, c);
+            double dum1 = -r.ee2(a, ap, bp, c, s);
+            if (a == ap) dum1 += 2.0 * r.D1(s, bp, c);
+            if (bp == ap) dum1 += r.D1(s, a, c);
+            double dum2 = -r.ee2(c, ap, bp, b, s);
+            if (ap == c) dum2 += 2.0 * r.D1(s, bp, b);
+            if (bp == ap) dum2 += r.D1(s, c, b);
+            Dm += -fbc * dum1 + fca * dum2;
+            for (int d = 1; d <= n; ++d)
+                for (int ie = 1; ie <= n; ++ie) {
+                    double e1 = -r.eee2(c, ie, a, ap, bp, d, s) - r.eee2(a, ap, bp, d, c, ie, s);
+                    if (ap == a) e1 += 2.0 * (r.ee2(c, ie, bp, d, s) + r.ee2(bp, d, c, ie, s));
+                    if (bp == ap) e1 += r.ee2(c, ie, a, d, s) + r.ee2(a, d, c, ie, s);
+                    if (ap == c) {
+                        e1 -= r.ee2(a, ie, bp, d, s);
+                        if (ie == a) e1 += 2.0 * r.D1(s, bp, d);
+                    }
+                    if (bp == ie) {
+                        e1 += r.ee2(a, ap, c, d, s);
+                        if (ap == a) e1 -= 2.0 * r.D1(s, c, d);
+                    }
+                    double e2 = -r.eee2(c, ie, d, ap, bp, b, s) - r.eee2(d, ap, bp, b, c, ie, s);
+                    if (ap == d) e2 += 2.0 * (r.ee2(c, ie, bp, b, s) + r.ee2(bp, b, c, ie, s));
+                    if (bp == ap) e2 += r.ee2(c, ie, d, b, s) + r.ee2(d, b, c, ie, s);
+                    if (ap == c) {
+                        e2 -= r.ee2(d, ie, bp, b, s);
+                        if (d == ie) e2 += 2.0 * r.D1(s, bp, b);
+                    }
+                    if (bp == ie) {
+                        e2 += r.ee2(d, ap, c, b, s);
+                        if (d == ap) e2 -= 2.0 * r.D1(s, c, b);
+                    }
+                    Dm += -0.5 * ATWO(c, ie, b, d) * e1 + 0.5 * ATWO(c, ie, d, a) * e2;
+                }
+        }
+        O5(koopaa, s, bp, ap, a, b) = A;
+        O5(koopbb, s, bp, ap, a, b) = Dm;
+    }
+}
+
+// src/koop_matrices.F90:546-571 koopman0pE, F (koopab).  Thread per (a,b).
+__global__ void k_koop0p_f(Rdm r, const double *atwo, const double *f, int ncore, double *koopab) {
+    const int n = r.n, M = r.M;
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * n) return;
+    int a = t % n + 1, b = t / n + 1;
+    for (int s = 1; s <= M; ++s) {
+        double acc = 0.0;
+        for (int c = 1; c <= n; ++c) {
+            acc += 2.0 * (FF(c, a) * r.D1(s, c, b) - FF(b, c) * r.D1(s, a, c));
+            for (int d = 1; d <= n; ++d)
+                for (int ie = 1; ie <= n; ++ie) {
+                    double dum1 = r.ee2(c, ie, d, b, s) + r.ee2(d, b, c, ie, s);
+                    double dum2 = r.ee2(a, ie, c, d, s) + r.ee2(c, d, a, ie, s);
+                    acc += ATWO(c, ie, d, a) * dum1 - ATWO(b, ie, c, d) * dum2;
+                }
+        }
+        O3(koopab, s, a, b) = acc;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// src/koopro4QD.F90:4231-4299 bbmat.  Thread per (ap,bp,cp,a).  The EA part
+// multiplies by aj, not by the modified f (reference quirk kept).
+__global__ void k_bbmat(Rdm r, const double *atwo, const double *f, const double *aj, int ncore, double *bmat,
+                        double *btmat) {
+    const int n = r.n, M = r.M;
+    ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (ll)n * n * n * n) return;
+    int x[4];
+    decode(t, n, 4, x);
+    const int ap = x[0], bp = x[1], cp = x[2], a = x[3];
+    for (int s = 1; s <= M; ++s) {
+        double B = 0.0, Bt = 0.0;
+        for (int c = 1; c <= n; ++c) {
+            B -= FF(c, a) * r.ee2(cp, ap, bp, c, s);
+            Bt += AJ(c, a) * r.ee2tr(cp, ap, bp, c, s);
+            for (int ie = 1; ie <= n; ++ie)
+                for (int ief = 1; ief <= n; ++ief) {
+                    double dint = ATWO(a, ie, c, ief);
+                    B -= r.eee2(cp, ap, bp, ie, c, ief, s) * dint;
+                    Bt += r.eee2t(cp, ap, bp, ie, c, ief, s) * dint;
+                }
+        }
+        O5(bmat, s, ap, bp, cp, a) = B;
+        O5(btmat, s, ap, bp, cp, a) = Bt;
+    }
+}
+
+// src/koopro4QD.F90:4301-4397 bcmat.  Thread per (ap,a,b,c); the reference's
+// d loop is the reduction.
+__global__ void k_bcmat(Rdm r, const double *atwo, const double *f, int ncore, double *cmat, double *ctmat) {
+    const int n = r.n, M = r.M;
+    ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (ll)n * n * n * n) return;
+    int x[4];
+    decode(t, n, 4, x);
+    const int ap = x[0], a = x[1], b = x[2], c = x[3];
+    for (int s = 1; s <= M; ++s) {
+        double C = 0.0, Ct = 0.0;
+        for (int d = 1; d <= n; ++d) {
+            double fda = FF(d, a), fcd = FF(c, d), fbd = FF(b, d);
+            C += fda * r.ee2(ap, b, d, c, s) - fcd * r.ee2(ap, b, a, d, s) - fbd * r.ee2(ap, d, a, c, s);
+            Ct += fda * r.ee2t(ap, b, d, c, s) - fcd * r.ee2t(ap, b, a, d, s) + fbd * r.ee2t(ap, d, a, c, s);
+            for (int ie = 1; ie <= n; ++ie) {
+                double dint1 = ATWO(c, ie, d, a), dint2 = ATWO(d, ie, ie, a);
+                double dint3 = ATWO(c, d, d, ie), dint4 = ATWO(b, d, d, ie);
+                C += r.ee2(ap, b, d, ie, s) * dint1 -
+                     0.5 * (r.ee2(ap, b, d, c, s) * dint2 + r.ee2(ap, b, a, ie, s) * dint3 - r.ee2(ap, ie, a, c, s) * dint4);
+                Ct += r.ee2t(ap, b, d, ie, s) * dint1 -
+                      0.5 * (r.ee2t(ap, b, d, c, s) * dint2 + r.ee2t(ap, b, a, ie, s) * dint3 -
+                             r.ee2t(ap, ie, a, c, s) * dint4);
+                for (int ief = 1; ief <= n; ++ief) {
+                    double di1 = ATWO(d, ief, ie, a), di2 = ATWO(d, ief, c, ie), di3 = ATWO(d, ief, b, ie);
+                    C += r.eee2(ap, b, d, ief, ie, c, s) * di1 - r.eee2(ap, b, d, ief, a, ie, s) * di2 -
+                         r.eee2(ap, ie, d, ief, a, c, s) * di3;
+                    Ct += r.eee2tl(ap, b, d, ief, ie, c, s) * di1 - r.eee2tl(ap, b, d, ief, a, ie, s) * di2 +
+                          r.eee2tl(ap, ie, d, ief, a, c, s) * di3;
+                }
+            }
+        }
+        O5(cmat, s, ap, a, b, c) = C;
+        O5(ctmat, s, ap, a, b, c) = Ct;
+    }
+}
+
+// src/koopro4QD.F90:4399-4459 bdmat.  Thread per (ap,a); EA part uses aj.
+__global__ void k_bdmat(Rdm r, const double *atwo, const double *f, const double *aj, int ncore, double *dmat,
+                        double *dtmat) {
+    const int n = r.n, M = r.M;
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * n) return;
+    int ap = t % n + 1, a = t / n + 1;
+    for (int s = 1; s <= M; ++s) {
+        double D = 0.0, Dt = 0.0;
+        for (int c = 1; c <= n; ++c) {
+            D -= FF(c, a) * r.D1(s, ap, c);
+            double dum = -r.D1(s, ap, c);
+            if (ap == c) dum += 2.0;
+            Dt += AJ(c, a) * dum;
+            for (int ie = 1; ie <= n; ++ie)
+                for (int ief = 1; ief <= n; ++ief) {
+                    double dint = ATWO(a, ie, c, ief);
+                    D -= r.ee2(ap, ie, c, ief, s) * dint;
+                    Dt += r.ee2t(ap, ie, c, ief, s) * dint;
+                }
+        }
+        O3(dmat, s, ap, a) = D;
+        O3(dtmat, s, ap, a) = Dt;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host launchers.
+static inline unsigned blocks_for(ll work, int tpb) { return (unsigned)((work + tpb - 1) / tpb); }
+
+void launch_build_f(double *f, const double *aj, const double *atwo, int n, int ncore, int mode, cudaStream_t st) {
+    k_build_f<<<blocks_for((ll)n * n, 128), 128, 0, st>>>(f, aj, atwo, n, ncore, mode);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+
+void launch_bro3(const Rdm &r, double *daaa, int nele, cudaStream_t st) {
+    ll n6 = (ll)r.n * r.n * r.n * r.n * r.n * r.n;
+    k_bro3<<<blocks_for(n6, 256), 256, 0, st>>>(r, daaa, 1.0 / (double)(nele - 3));
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+void launch_bro2(const Rdm &r, double *taa, int nele, cudaStream_t st) {
+    ll n4 = (ll)r.n * r.n * r.n * r.n;
+    k_bro2<<<blocks_for(n4, 256), 256, 0, st>>>(r, taa, 1.0 / (double)(nele - 2));
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+void launch_bro1(const Rdm &r, double *dal, int nele, cudaStream_t st) {
+    k_bro1<<<blocks_for((ll)r.n * r.n, 128), 128, 0, st>>>(r, dal, 1.0 / (double)(nele - 1));
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+
+void launch_aj_atwo(const double *oneint, const double *L, int Q, int n, int ncore, int norb, double *atwo,
+                    double *aj, cudaStream_t st) {
+    cudaMemcpyAsync(aj, oneint, sizeof(double) * (size_t)norb * (norb + 1) / 2, cudaMemcpyDeviceToDevice, st);
+    k_aj<<<blocks_for((ll)n * n, 64), 64, 0, st>>>(oneint, L, Q, n, ncore, aj);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    ll n4 = (ll)n * n * n * n;
+    k_atwo<<<blocks_for(n4, 128), 128, 0, st>>>(L, Q, n, ncore, atwo);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+
+void launch_koopE(const Rdm &r, const double *atwo, const double *f, int ncore, double *ip, double *ea,
+                  cudaStream_t st) {
+    k_koopE<<<blocks_for((ll)r.n * r.n, 64), 64, 0, st>>>(r, atwo, f, ncore, ip, ea);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+void launch_hrdm(const Rdm &r, double *hrdm, cudaStream_t st) {
+    ll n4 = (ll)r.n * r.n * r.n * r.n;
+    k_hrdm<<<blocks_for(n4, 256), 256, 0, st>>>(r, hrdm);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+void launch_koop2E(const Rdm &r, const double *atwo, const double *f, int ncore, double *ip2, double *ea2,
+                   cudaStream_t st) {
+    ll n4 = (ll)r.n * r.n * r.n * r.n;
+    k_koop2E_ip<<<blocks_for(n4, 64), 64, 0, st>>>(r, atwo, f, ncore, ip2);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    k_koop2E_ea<<<blocks_for(n4, 64), 64, 0, st>>>(r, atwo, f, ncore, ea2);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+void launch_koop0p(const Rdm &r, const double *atwo, const double *f, int ncore, double *gk0pa, double *gk0pd,
+                   double *gk0pf, cudaStream_t st) {
+    ll n4 = (ll)r.n * r.n * r.n * r.n;
+    k_koop0p_ad<<<blocks_for(n4, 64), 64, 0, st>>>(r, atwo, f, ncore, gk0pa, gk0pd);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    k_koop0p_f<<<blocks_for((ll)r.n * r.n, 64), 64, 0, st>>>(r, atwo, f, ncore, gk0pf);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+void launch_bbmat(const Rdm &r, const double *atwo, const double *f, const double *aj, int ncore, double *b,
+                  double *bt, cudaStream_t st) {
+    ll n4 = (ll)r.n * r.n * r.n * r.n;
+    k_bbmat<<<blocks_for(n4, 64), 64, 0, st>>>(r, atwo, f, aj, ncore, b, bt);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+void launch_bcmat(const Rdm &r, const double *atwo, const double *f, int ncore, double *c, double *ct,
+                  cudaStream_t st) {
+    ll n4 = (ll)r.n * r.n * r.n * r.n;
+    k_bcmat<<<blocks_for(n4, 64), 64, 0, st>>>(r, atwo, f, ncore, c, ct);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+void launch_bdmat(const Rdm &r, const double *atwo, const double *f, const double *aj, int ncore, double *d,
+                  double *dt, cudaStream_t st) {
+    k_bdmat<<<blocks_for((ll)r.n * r.n, 64), 64, 0, st>>>(r, atwo, f, aj, ncore, d, dt);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+
+}  // namespace nvpt

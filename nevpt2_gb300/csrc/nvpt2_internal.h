@@ -1,0 +1,37 @@
+// Internal declarations shared by the CUDA translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <atomic>
+#include <cstdint>
+#include <string>
+#include "eexx.cuh"
+
+namespace nvpt {
+
+// Kernels launched by this library since load (all contexts).
+extern std::atomic<long long> g_launches;
+
+void launch_build_f(double *f, const double *aj, const double *atwo, int n, int ncore, int mode, cudaStream_t st);
+void launch_bro3(const Rdm &r, double *daaa, int nele, cudaStream_t st);
+void launch_bro2(const Rdm &r, double *taa, int nele, cudaStream_t st);
+void launch_bro1(const Rdm &r, double *dal, int nele, cudaStream_t st);
+void launch_aj_atwo(const double *oneint, const double *L, int Q, int n, int ncore, int norb, double *atwo,
+                    double *aj, cudaStream_t st);
+void launch_koopE(const Rdm &r, const double *atwo, const double *f, int ncore, double *ip, double *ea,
+                  cudaStream_t st);
+void launch_hrdm(const Rdm &r, double *hrdm, cudaStream_t st);
+void launch_koop2E(const Rdm &r, const double *atwo, const double *f, int ncore, double *ip2, double *ea2,
+                   cudaStream_t st);
+void launch_koop0p(const Rdm &r, const double *atwo, const double *f, int ncore, double *gk0pa, double *gk0pd,
+                   double *gk0pf, cudaStream_t st);
+void launch_bbmat(const Rdm &r, const double *atwo, const double *f, const double *aj, int ncore, double *b,
+                  double *bt, cudaStream_t st);
+void launch_bcmat(const Rdm &r, const double *atwo, const double *f, int ncore, double *c, double *ct,
+                  cudaStream_t st);
+void launch_bdmat(const Rdm &r, const double *atwo, const double *f, const double *aj, int ncore, double *d,
+                  double *dt, cudaStream_t st);
+void launch_bamat_direct(const Rdm &r, const double *atwo, const double *f, int ncore, double *amat, double *atmat,
+                         cudaStream_t st);
+void launch_ord8(const int64_t *in8, int64_t *out8, int64_t *lindex, long long count, cudaStream_t st);
+
+}  // namespace nvpt

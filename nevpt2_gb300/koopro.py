@@ -1,0 +1,133 @@
+"""Host-side mirror of the reference's stage-1 subroutines (koopro4QD.x).
+
+Each function has the name, argument meaning and array layout of the Fortran
+subroutine it replaces (numpy arrays in Fortran order with the reference's
+shapes: state index first, ro4 state last) and runs on the GPU through the C
+ABI.  Results the reference writes to nevpt.h5 are returned as arrays keyed
+by their dataset names.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from ._native import Context, ptr
+
+_ctx: Context | None = None
+
+
+def context() -> Context:
+    global _ctx
+    if _ctx is None:
+        _ctx = Context(0)
+    return _ctx
+
+
+def _f(a) -> np.ndarray:
+    a = np.asarray(a, dtype=np.float64)
+    return a if a.flags.f_contiguous else np.asfortranarray(a)
+
+
+def _z(*shape) -> np.ndarray:
+    return np.zeros(shape, order="F")
+
+
+def nwords(nact: int) -> int:
+    return int(context()._lib.nvpt_nwords(nact))
+
+
+def ord8(nact: int, tuples) -> tuple[np.ndarray, np.ndarray]:
+    """src/ord_utils.F90:71 ord8 on the device for an (N,8) array of 1-based
+    tuples; returns ((N,8) sorted key + partner, (N,) lindice)."""
+    t = np.ascontiguousarray(tuples, dtype=np.int64).reshape(-1, 8)
+    out = np.zeros_like(t)
+    lind = np.zeros(t.shape[0], np.int64)
+    context().call("nvpt_ord8", nact, t.shape[0], ptr(t), ptr(out), ptr(lind))
+    return out, lind
+
+
+def bro3(ro4, nact: int, nele: int, metat: int) -> np.ndarray:
+    """src/koopro4QD.F90:4881 bro3 -> daaa(metat, n^6)."""
+    out = _z(metat, *(nact,) * 6)
+    context().call("nvpt_bro3", ptr(_f(ro4)), ptr(out), nact, nele, metat)
+    return out
+
+
+def bro2(daaa, nact: int, nele: int, metat: int) -> np.ndarray:
+    out = _z(metat, *(nact,) * 4)
+    context().call("nvpt_bro2", ptr(_f(daaa)), ptr(out), nact, nele, metat)
+    return out
+
+
+def bro1(taa, nact: int, nele: int, metat: int) -> np.ndarray:
+    out = _z(metat, nact, nact)
+    context().call("nvpt_bro1", ptr(_f(taa)), ptr(out), nact, nele, metat)
+    return out
+
+
+def get_aj_atwo(nact: int, ncore: int, norb: int, oneint, cholesky_array):
+    """src/koopro4QD.F90:3900 get_aj_atwo on the Cholesky integral path."""
+    atwo = _z(nact, nact, nact, nact)
+    aj = np.zeros(norb * (norb + 1) // 2)
+    L = _f(cholesky_array)
+    context().call("nvpt_get_aj_atwo", ptr(atwo), nact, ncore, norb, ptr(aj), ptr(_f(oneint)), ptr(L), L.shape[0])
+    return atwo, aj
+
+
+def koop_matrices_ctl(metat: int, nact: int, ncore: int, atwo, daaa, taa, dal, f, aj) -> dict:
+    """src/koop_matrices.F90:16 koop_matrices_ctl.  ``f`` is updated in place."""
+    n, M = nact, metat
+    out = {"1-IPKO": _z(M, n, n), "1-EAKO": _z(M, n, n), "2-HRDM": _z(M, n, n, n, n), "2-IPKO": _z(M, n, n, n, n),
+           "2-EAKO": _z(M, n, n, n, n), "gk0pa": _z(M, n, n, n, n), "gk0pd": _z(M, n, n, n, n), "gk0pf": _z(M, n, n)}
+    context().call("nvpt_koop_matrices_ctl", M, n, ncore, ptr(_f(atwo)), ptr(_f(daaa)), ptr(_f(taa)), ptr(_f(dal)),
+                   ptr(f), ptr(_f(aj)), *[ptr(out[k]) for k in ("1-IPKO", "1-EAKO", "2-HRDM", "2-IPKO", "2-EAKO",
+                                                               "gk0pa", "gk0pd", "gk0pf")])
+    return out
+
+
+def bamat(atwo, ro4, daaa, taa, dal, nact: int, ncore: int, f, aj, norb: int, metat: int, nsym: int = 1):
+    """src/koopro4QD.F90:3974 bamat -> (amat "amatIP", atmat "amatEA")."""
+    amat, atmat = _z(metat, *(nact,) * 6), _z(metat, *(nact,) * 6)
+    context().call("nvpt_bamat", ptr(amat), ptr(atmat), ptr(_f(atwo)), ptr(_f(ro4)), ptr(_f(daaa)), ptr(_f(taa)),
+                   ptr(_f(dal)), nact, ncore, ptr(f), ptr(_f(aj)), norb, metat, nsym)
+    return amat, atmat
+
+
+def bbmat(atwo, daaa, taa, dal, nact: int, ncore: int, f, aj, metat: int):
+    b, bt = _z(metat, *(nact,) * 4), _z(metat, *(nact,) * 4)
+    context().call("nvpt_bbmat", ptr(_f(atwo)), ptr(b), ptr(bt), ptr(_f(daaa)), ptr(_f(taa)), ptr(_f(dal)), nact,
+                   ncore, ptr(f), ptr(_f(aj)), metat)
+    return b, bt
+
+
+def bcmat(atwo, daaa, taa, dal, nact: int, ncore: int, f, aj, metat: int):
+    c, ct = _z(metat, *(nact,) * 4), _z(metat, *(nact,) * 4)
+    context().call("nvpt_bcmat", ptr(_f(atwo)), ptr(c), ptr(ct), ptr(_f(daaa)), ptr(_f(taa)), ptr(_f(dal)), nact,
+                   ncore, ptr(f), ptr(_f(aj)), metat)
+    return c, ct
+
+
+def bdmat(atwo, taa, dal, nact: int, ncore: int, f, aj, metat: int):
+    d, dt = _z(metat, nact, nact), _z(metat, nact, nact)
+    context().call("nvpt_bdmat", ptr(_f(atwo)), ptr(d), ptr(dt), ptr(_f(taa)), ptr(_f(dal)), nact, ncore, ptr(f),
+                   ptr(_f(aj)), metat)
+    return d, dt
+
+
+def koopro4QD(problem) -> dict:
+    """Stage 1 of one problem, in the reference driver's order
+    (src/koopro4QD.F90:270-423): bro3/bro2/bro1 from the packed 4-RDM,
+    get_aj_atwo, koop_matrices_ctl, bamat, bbmat, bcmat, bdmat."""
+    p = problem
+    n, M, nc, norb = p.nact, p.metat, p.ncore, p.norb
+    daaa = bro3(p.ro4, n, p.nele, M)
+    taa = bro2(daaa, n, p.nele, M)
+    dal = bro1(taa, n, p.nele, M)
+    atwo, aj = get_aj_atwo(n, nc, norb, p.oneint, p.chol)
+    f = np.zeros(norb * (norb + 1) // 2)
+    out = koop_matrices_ctl(M, n, nc, atwo, daaa, taa, dal, f, aj)
+    out.update({"3-RDM": daaa, "2-RDM": taa, "1-RDM": dal, "atwo": atwo, "aj": aj})
+    out["amatIP"], out["amatEA"] = bamat(atwo, p.ro4, daaa, taa, dal, n, nc, f, aj, norb, M)
+    out["bmatIP"], out["bmatEA"] = bbmat(atwo, daaa, taa, dal, n, nc, f, aj, M)
+    out["cmatIP"], out["cmatEA"] = bcmat(atwo, daaa, taa, dal, n, nc, f, aj, M)
+    out["dmatIP"], out["dmatEA"] = bdmat(atwo, taa, dal, n, nc, f, aj, M)
+    return out

@@ -1,0 +1,943 @@
+/*
+ * CPU oracle for the Koopmans-matrix stage of NEVPT2 (stage 1 of the reference,
+ * `koopro4QD.x`).  TEST INFRASTRUCTURE ONLY: this file is the checker that the
+ * CUDA library is compared against, and the scalar CPU baseline that the bench
+ * reports beside the GPU numbers.  Nothing in the product links it.
+ *
+ * It restates, loop for loop, these reference routines (paths relative to the
+ * qcscine/nevpt2 source tree):
+ *   src/indices_norm.F90:31-55   initialize_indices_norm (lindi/lindj/lindk/normind)
+ *   src/indices_norm.F90:64-106  lindice, norm
+ *   src/ord_utils.F90:16-68      ord9
+ *   src/ord_utils.F90:71-129     ord8
+ *   src/eexx_functions.F90:25-225 eeee, eeeet, eee2, eee2t, eee2tl, ee2, ee2t,
+ *                                ee2tr, ro3t, ro2t
+ *   src/koop_matrices.F90:16-619 koop_matrices_ctl, koopE, ro2t loop (2-HRDM),
+ *                                koop2E, koopman0pE, fdiff_F
+ *   src/koopro4QD.F90:3900-3971  get_aj_atwo (Cholesky/DF integral path,
+ *                                src/ijkl_utils.F90:637-688 ai_cholesky)
+ *   src/koopro4QD.F90:3974-4229  bamat (C1 branch, :4008-4104)
+ *   src/koopro4QD.F90:4231-4459  bbmat, bcmat, bdmat
+ *   src/koopro4QD.F90:4881-5049  bro3, bro2, bro1
+ *   src/koopro4QD.F90:5053-5112  fdiff
+ *
+ * Parity status: the reference ships no tests, fixtures or golden vectors and
+ * cannot be compiled in this container (Fortran, HDF5 and MOLCAS are absent),
+ * so this restatement is "parity unpinned" against the reference binary.  It is
+ * pinned by the reference's own run-time invariants (fdiff: B == C^T, fdiff_F:
+ * F == 0, partial-trace chain bro3/bro2/bro1, trace of the 1-RDM) and by a
+ * brute-force second-quantised evaluation of <E..E> on tiny active spaces.
+ *
+ * Array conventions follow the reference exactly: Fortran column-major,
+ * 1-based indices, state index first (fastest), except ro4(W,n,n,n,n,M) where
+ * the state is last.  f/aj are lower-triangle packed with
+ * indice(i,j) = max*(max-1)/2 + min over the full orbital range.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include <stdio.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+typedef int64_t I;
+
+/* ------------------------------------------------------------------------ */
+/* Column-major addressing helpers (1-based indices, state-first layouts).   */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    I n, M, W;
+    I *lindi, *lindj, *lindk, *normind; /* normind(n,n,n,n) column-major */
+    const double *d1, *d2, *d3, *ro4;   /* dal, taa, daaa, ro4            */
+} orc_ctx;
+
+#define D1(c, s, a, b) ((c)->d1[((s)-1) + (c)->M * (((a)-1) + (c)->n * ((b)-1))])
+#define D2(c, s, a, b, cc, d)                                                  \
+    ((c)->d2[((s)-1) +                                                         \
+             (c)->M * (((a)-1) +                                               \
+                       (c)->n * (((b)-1) + (c)->n * (((cc)-1) + (c)->n * ((d)-1))))])
+#define D3(c, s, a, b, cc, d, e, f)                                             \
+    ((c)->d3[((s)-1) + (c)->M * (((a)-1) + (c)->n * (((b)-1) + (c)->n * (((cc)-1) + \
+             (c)->n * (((d)-1) + (c)->n * (((e)-1) + (c)->n * ((f)-1))))))])
+#define NORMIND(c, i, j, k, l)                                                 \
+    ((c)->normind[((i)-1) + (c)->n * (((j)-1) + (c)->n * (((k)-1) + (c)->n * ((l)-1)))])
+
+static inline I o_indice(I i, I j) {
+    I mx = i > j ? i : j, mn = i > j ? j : i;
+    return mx * (mx - 1) / 2 + mn;
+}
+
+/* indices_norm.F90:76-106 norm_array: selection sort descending, then pack. */
+static I o_norm(I a, I b, I c, I d) {
+    I nv[4] = {a, b, c, d};
+    for (int i = 0; i < 4; ++i) {
+        I imax = nv[i];
+        int jmax = i;
+        for (int j = i + 1; j < 4; ++j)
+            if (nv[j] > imax) { imax = nv[j]; jmax = j; }
+        if (jmax != i) { I t = nv[i]; nv[i] = nv[jmax]; nv[jmax] = t; }
+    }
+    return (nv[0] - 1) * nv[0] * (nv[0] + 1) * (nv[0] + 2) / 24 +
+           (nv[1] - 1) * nv[1] * (nv[1] + 1) / 6 + nv[2] * (nv[2] - 1) / 2 + nv[3];
+}
+
+/* indices_norm.F90:31-55 */
+static void o_init(orc_ctx *c, I n, I M) {
+    c->n = n;
+    c->M = M;
+    c->lindi = (I *)malloc(sizeof(I) * n);
+    c->lindj = (I *)malloc(sizeof(I) * n);
+    c->lindk = (I *)malloc(sizeof(I) * n);
+    c->normind = (I *)malloc(sizeof(I) * n * n * n * n);
+    for (I i = 1; i <= n; ++i) {
+        c->lindi[i - 1] = (i - 1) * i * (i + 1) * (i + 2) / 24;
+        c->lindj[i - 1] = (i - 1) * i * (i + 1) / 6;
+        c->lindk[i - 1] = (i - 1) * i / 2;
+        for (I j = 1; j <= n; ++j)
+            for (I k = 1; k <= n; ++k)
+                for (I l = 1; l <= n; ++l) NORMIND(c, i, j, k, l) = o_norm(i, j, k, l);
+    }
+    c->W = n * (n + 1) * (n + 2) * (n + 3) / 24;
+}
+
+static void o_free(orc_ctx *c) {
+    free(c->lindi);
+    free(c->lindj);
+    free(c->lindk);
+    free(c->normind);
+}
+
+/* indices_norm.F90:64-72 */
+static inline I o_lindice(const orc_ctx *c, I i, I j, I k, I l) {
+    return c->lindi[i - 1] + c->lindj[j - 1] + c->lindk[k - 1] + l;
+}
+
+/* ord_utils.F90:71-129 ord8: pick the key group, selection-sort it
+ * descending (first maximum wins), apply every swap to the partner group. */
+static inline void o_ord8(const orc_ctx *c, I a1, I c1, I e1, I g1, I a2, I c2, I e2, I g2,
+                          I out[8]) {
+    I nv1[4], nv2[4];
+    if (NORMIND(c, a1, c1, e1, g1) >= NORMIND(c, a2, c2, e2, g2)) {
+        nv1[0] = a1; nv1[1] = c1; nv1[2] = e1; nv1[3] = g1;
+        nv2[0] = a2; nv2[1] = c2; nv2[2] = e2; nv2[3] = g2;
+    } else {
+        nv1[0] = a2; nv1[1] = c2; nv1[2] = e2; nv1[3] = g2;
+        nv2[0] = a1; nv2[1] = c1; nv2[2] = e1; nv2[3] = g1;
+    }
+    for (int i = 0; i < 4; ++i) {
+        I imax = nv1[i];
+        int jmax = i;
+        for (int j = i + 1; j < 4; ++j)
+            if (nv1[j] > imax) { imax = nv1[j]; jmax = j; }
+        if (jmax != i) {
+            I t = nv1[i]; nv1[i] = nv1[jmax]; nv1[jmax] = t;
+            t = nv2[i]; nv2[i] = nv2[jmax]; nv2[jmax] = t;
+        }
+    }
+    for (int i = 0; i < 4; ++i) { out[i] = nv1[i]; out[4 + i] = nv2[i]; }
+}
+
+/* ord_utils.F90:16-68 ord9: same key choice; the inner loop swaps eagerly on
+ * every strictly larger element it meets (different result on ties). */
+static inline void o_ord9(const orc_ctx *c, I a1, I c1, I e1, I g1, I a2, I c2, I e2, I g2,
+                          I out[8]) {
+    I nv1[4], nv2[4];
+    if (NORMIND(c, a1, c1, e1, g1) >= NORMIND(c, a2, c2, e2, g2)) {
+        nv1[0] = a1; nv1[1] = c1; nv1[2] = e1; nv1[3] = g1;
+        nv2[0] = a2; nv2[1] = c2; nv2[2] = e2; nv2[3] = g2;
+    } else {
+        nv1[0] = a2; nv1[1] = c2; nv1[2] = e2; nv1[3] = g2;
+        nv2[0] = a1; nv2[1] = c1; nv2[2] = e1; nv2[3] = g1;
+    }
+    for (int i = 0; i < 4; ++i) {
+        I imax = nv1[i];
+        for (int j = i + 1; j < 4; ++j) {
+            if (nv1[j] > imax) {
+                I n = imax;
+                imax = nv1[j];
+                nv1[j] = n;
+                n = nv2[i]; nv2[i] = nv2[j]; nv2[j] = n;
+            }
+            nv1[i] = imax;
+        }
+    }
+    for (int i = 0; i < 4; ++i) { out[i] = nv1[i]; out[4 + i] = nv2[i]; }
+}
+
+static inline double o_ro4(const orc_ctx *c, I ind, I i5, I i6, I i7, I i8, I s) {
+    I n = c->n;
+    return c->ro4[(ind - 1) +
+                  c->W * ((i5 - 1) + n * ((i6 - 1) + n * ((i7 - 1) + n * ((i8 - 1) + n * (s - 1)))))];
+}
+
+/* eexx_functions.F90:79-94 */
+static inline double o_eee2(const orc_ctx *c, I a, I b, I cc, I d, I e, I f, I s) {
+    double r = D3(c, s, a, cc, e, b, d, f);
+    if (e == d) r += D2(c, s, a, cc, b, f);
+    if (e == b) r += D2(c, s, a, cc, f, d);
+    if (b == cc) r += D2(c, s, a, e, d, f);
+    if (b == cc && e == d) r += D1(c, s, a, f);
+    return r;
+}
+
+/* eexx_functions.F90:125-135 */
+static inline double o_ee2(const orc_ctx *c, I a, I b, I cc, I d, I s) {
+    double r = D2(c, s, a, cc, b, d);
+    if (b == cc) r += D1(c, s, a, d);
+    return r;
+}
+
+/* eexx_functions.F90:138-148 */
+static inline double o_ee2t(const orc_ctx *c, I a, I b, I cc, I d, I s) {
+    double r = -o_ee2(c, b, a, cc, d, s);
+    if (a == b) r += 2.0 * D1(c, s, cc, d);
+    return r;
+}
+
+/* eexx_functions.F90:151-161 */
+static inline double o_ee2tr(const orc_ctx *c, I a, I b, I cc, I d, I s) {
+    double r = -o_ee2(c, a, b, d, cc, s);
+    if (cc == d) r += 2.0 * D1(c, s, a, b);
+    return r;
+}
+
+/* eexx_functions.F90:97-108 */
+static inline double o_eee2t(const orc_ctx *c, I a, I b, I cc, I d, I e, I f, I s) {
+    double r = -o_eee2(c, a, b, d, cc, e, f, s);
+    if (cc == d) r += 2.0 * o_ee2(c, a, b, e, f, s);
+    return r;
+}
+
+/* eexx_functions.F90:111-122 */
+static inline double o_eee2tl(const orc_ctx *c, I a, I b, I cc, I d, I e, I f, I s) {
+    double r = -o_eee2(c, b, a, cc, d, e, f, s);
+    if (a == b) r += 2.0 * o_ee2(c, cc, d, e, f, s);
+    return r;
+}
+
+/* eexx_functions.F90:25-61 */
+static inline double o_eeee(const orc_ctx *c, I a, I b, I cc, I d, I e, I f, I g, I h, I s) {
+    I o[8];
+    o_ord8(c, a, cc, e, g, b, d, f, h, o);
+    I ind = o_lindice(c, o[0], o[1], o[2], o[3]);
+    double r = o_ro4(c, ind, o[4], o[5], o[6], o[7], s);
+    if (b == cc) r += D3(c, s, a, e, g, d, f, h);
+    if (b == e) r += D3(c, s, a, cc, g, f, d, h);
+    if (b == g) r += D3(c, s, a, cc, e, h, d, f);
+    if (d == e) r += D3(c, s, a, g, cc, b, h, f);
+    if (d == g) r += D3(c, s, a, cc, e, b, h, f);
+    if (f == g) r += D3(c, s, a, e, cc, b, h, d);
+    if (b == cc) {
+        if (d == e) r += D2(c, s, a, g, f, h);
+        if (d == g) r += D2(c, s, a, e, h, f);
+        if (f == g) r += D2(c, s, a, e, d, h);
+    }
+    if (b == e && d == g) r += D2(c, s, a, cc, f, h);
+    if (b == e && f == g) r += D2(c, s, a, cc, h, d);
+    if (b == g && d == e) r += D2(c, s, a, cc, h, f);
+    if (d == e && f == g) r += D2(c, s, a, cc, b, h);
+    if (b == cc && d == e && f == g) r += D1(c, s, a, h);
+    return r;
+}
+
+/* eexx_functions.F90:64-75 */
+static inline double o_eeeet(const orc_ctx *c, I a, I b, I cc, I d, I e, I f, I g, I h, I s) {
+    double r = -o_eeee(c, a, b, d, cc, e, f, g, h, s);
+    if (cc == d) r += 2.0 * o_eee2(c, a, b, e, f, g, h, s);
+    return r;
+}
+
+/* eexx_functions.F90:164-207 (d3/d2/d1 are the arrays the caller passes) */
+static double o_ro3t(const orc_ctx *c, I a, I b, I cc, I ap, I bp, I cp, I s) {
+    double r = -D3(c, s, ap, bp, cp, a, b, cc);
+    if (ap == a) r += 2.0 * D2(c, s, bp, cp, b, cc);
+    if (bp == b) r += 2.0 * D2(c, s, ap, cp, a, cc);
+    if (cp == cc) r += 2.0 * D2(c, s, ap, bp, a, b);
+    if (bp == cc) r -= D2(c, s, ap, cp, a, b);
+    if (ap == cc) r -= D2(c, s, cp, bp, a, b);
+    if (cp == b) r -= D2(c, s, bp, ap, cc, a);
+    if (ap == b) r -= D2(c, s, bp, cp, a, cc);
+    if (cp == a) r -= D2(c, s, ap, bp, cc, b);
+    if (bp == a) r -= D2(c, s, ap, cp, b, cc);
+    if (cp == cc && bp == b) r -= 4.0 * D1(c, s, ap, a);
+    if (cp == b && bp == cc) r += 2.0 * D1(c, s, ap, a);
+    if (cp == cc && ap == a) r -= 4.0 * D1(c, s, bp, b);
+    if (cp == a && ap == cc) r += 2.0 * D1(c, s, bp, b);
+    if (ap == a && bp == b) r -= 4.0 * D1(c, s, cp, cc);
+    if (ap == b && bp == a) r += 2.0 * D1(c, s, cp, cc);
+    if (cp == cc && ap == b) r += 2.0 * D1(c, s, bp, a);
+    if (cp == b && ap == cc) r -= D1(c, s, bp, a);
+    if (cp == cc && bp == a) r += 2.0 * D1(c, s, ap, b);
+    if (cp == a && bp == cc) r -= D1(c, s, ap, b);
+    if (bp == b && ap == cc) r += 2.0 * D1(c, s, cp, a);
+    if (bp == cc && ap == b) r -= D1(c, s, cp, a);
+    if (bp == b && cp == a) r += 2.0 * D1(c, s, ap, cc);
+    if (bp == a && cp == b) r -= D1(c, s, ap, cc);
+    if (ap == a && cp == b) r += 2.0 * D1(c, s, bp, cc);
+    if (ap == b && cp == a) r -= D1(c, s, bp, cc);
+    if (ap == a && bp == cc) r += 2.0 * D1(c, s, cp, b);
+    if (ap == cc && bp == a) r -= D1(c, s, cp, b);
+    if (ap == a && bp == b && cp == cc) r += 8.0;
+    if (ap == b && bp == a && cp == cc) r -= 4.0;
+    if (ap == a && bp == cc && cp == b) r -= 4.0;
+    if (ap == cc && bp == b && cp == a) r -= 4.0;
+    if (ap == b && bp == cc && cp == a) r += 2.0;
+    if (ap == cc && bp == a && cp == b) r += 2.0;
+    return r;
+}
+
+/* eexx_functions.F90:210-225 */
+static inline double o_ro2t(const orc_ctx *c, I ap, I bp, I a, I b, I s) {
+    double r = D2(c, s, a, b, ap, bp);
+    if (ap == a) r -= 2.0 * D1(c, s, b, bp);
+    if (bp == b) r -= 2.0 * D1(c, s, a, ap);
+    if (ap == b) r += D1(c, s, a, bp);
+    if (bp == a) r += D1(c, s, b, ap);
+    if (ap == a && bp == b) r += 4.0;
+    if (ap == b && bp == a) r -= 2.0;
+    return r;
+}
+
+/* ======================================================================== */
+/* Exported entry points.  Every array is passed in the reference layout.    */
+/* ======================================================================== */
+
+/* Bit-exact integer kernels, exposed for the index-map tests. */
+I orc_nwords(I n) { return n * (n + 1) * (n + 2) * (n + 3) / 24; }
+
+void orc_index_tables(I n, I *lindi, I *lindj, I *lindk, I *normind) {
+    orc_ctx c;
+    o_init(&c, n, 1);
+    memcpy(lindi, c.lindi, sizeof(I) * n);
+    memcpy(lindj, c.lindj, sizeof(I) * n);
+    memcpy(lindk, c.lindk, sizeof(I) * n);
+    memcpy(normind, c.normind, sizeof(I) * n * n * n * n);
+    o_free(&c);
+}
+
+/* Apply ord8 (which=8) or ord9 (which=9) to `count` 8-tuples (1-based). */
+void orc_ord(I n, int which, I count, const I *in8, I *out8) {
+    orc_ctx c;
+    o_init(&c, n, 1);
+    for (I t = 0; t < count; ++t) {
+        const I *x = in8 + 8 * t;
+        if (which == 9)
+            o_ord9(&c, x[0], x[1], x[2], x[3], x[4], x[5], x[6], x[7], out8 + 8 * t);
+        else
+            o_ord8(&c, x[0], x[1], x[2], x[3], x[4], x[5], x[6], x[7], out8 + 8 * t);
+    }
+    o_free(&c);
+}
+
+/* koopro4QD.F90:4881-4959 bro3: daaa += sum_l ro4[ord8(i,j,k,l;ii,jj,kk,l)] / (nele-3).
+ * daaa is accumulated into (the reference zeroes it before the call). */
+void orc_bro3(const double *ro4, double *daaa, I nact, I nele, I metat) {
+    orc_ctx c;
+    o_init(&c, nact, metat);
+    c.ro4 = ro4;
+    I n = nact, M = metat;
+#pragma omp parallel for collapse(2) schedule(static)
+    for (I i = 1; i <= n; ++i)
+        for (I j = 1; j <= n; ++j)
+            for (I k = 1; k <= n; ++k)
+                for (I ii = 1; ii <= n; ++ii)
+                    for (I jj = 1; jj <= n; ++jj)
+                        for (I kk = 1; kk <= n; ++kk) {
+                            I base = M * ((i - 1) + n * ((j - 1) + n * ((k - 1) + n * ((ii - 1) + n * ((jj - 1) + n * (kk - 1))))));
+                            for (I ll = 1; ll <= n; ++ll) {
+                                I o[8];
+                                o_ord8(&c, i, j, k, ll, ii, jj, kk, ll, o);
+                                I ind = o_lindice(&c, o[0], o[1], o[2], o[3]);
+                                for (I s = 1; s <= M; ++s)
+                                    daaa[base + s - 1] += o_ro4(&c, ind, o[4], o[5], o[6], o[7], s);
+                            }
+                            for (I s = 1; s <= M; ++s) daaa[base + s - 1] = daaa[base + s - 1] / (double)(nele - 3);
+                        }
+    o_free(&c);
+}
+
+/* koopro4QD.F90:4961-5000 bro2 */
+void orc_bro2(const double *daaa, double *taa, I nact, I nele, I metat) {
+    orc_ctx c;
+    memset(&c, 0, sizeof c);
+    c.n = nact; c.M = metat; c.d3 = daaa;
+    I n = nact, M = metat;
+    for (I i = 1; i <= n; ++i)
+        for (I j = 1; j <= n; ++j)
+            for (I ii = 1; ii <= n; ++ii)
+                for (I jj = 1; jj <= n; ++jj) {
+                    I base = M * ((i - 1) + n * ((j - 1) + n * ((ii - 1) + n * (jj - 1))));
+                    for (I ll = 1; ll <= n; ++ll)
+                        for (I s = 1; s <= M; ++s) taa[base + s - 1] += D3(&c, s, i, j, ll, ii, jj, ll);
+                    for (I s = 1; s <= M; ++s) taa[base + s - 1] = taa[base + s - 1] / (double)(nele - 2);
+                }
+}
+
+/* koopro4QD.F90:5002-5049 bro1 */
+void orc_bro1(const double *taa, double *dal, I nact, I nele, I metat) {
+    orc_ctx c;
+    memset(&c, 0, sizeof c);
+    c.n = nact; c.M = metat; c.d2 = taa;
+    I n = nact, M = metat;
+    for (I i = 1; i <= n; ++i)
+        for (I j = 1; j <= n; ++j) {
+            I base = M * ((i - 1) + n * (j - 1));
+            for (I ll = 1; ll <= n; ++ll)
+                for (I s = 1; s <= M; ++s) dal[base + s - 1] += D2(&c, s, i, ll, j, ll);
+            for (I s = 1; s <= M; ++s) dal[base + s - 1] = dal[base + s - 1] / (double)(nele - 1);
+        }
+}
+
+/* ijkl_utils.F90:637-688 ai_cholesky: (ij|kl) = sum_Q L(Q,indice(i,j)) L(Q,indice(k,l)) */
+static inline double o_ai(const double *chol, I nchovec, I i, I j, I k, I l) {
+    const double *x = chol + nchovec * (o_indice(i, j) - 1);
+    const double *y = chol + nchovec * (o_indice(k, l) - 1);
+    double s = 0.0;
+    for (I q = 0; q < nchovec; ++q) s += x[q] * y[q];
+    return s;
+}
+
+double orc_ai(const double *chol, I nchovec, I i, I j, I k, I l) { return o_ai(chol, nchovec, i, j, k, l); }
+
+/* koopro4QD.F90:3900-3971 get_aj_atwo (Cholesky integrals). */
+void orc_get_aj_atwo(const double *oneint, const double *chol, I nchovec, I nact, I ncore, I norb,
+                     double *atwo, double *aj) {
+    I n = nact;
+    memcpy(aj, oneint, sizeof(double) * (size_t)(norb * (norb + 1) / 2));
+    for (I a = 1; a <= n; ++a) {
+        I ac = a + ncore;
+        for (I b = a; b <= n; ++b) {
+            I bc = b + ncore;
+            I jab = o_indice(ac, bc);
+            for (I j = 1; j <= ncore; ++j)
+                aj[jab - 1] = aj[jab - 1] + 2.0 * o_ai(chol, nchovec, ac, bc, j, j) - o_ai(chol, nchovec, ac, j, j, bc);
+        }
+    }
+#pragma omp parallel for collapse(2)
+    for (I i = 1; i <= n; ++i)
+        for (I j = 1; j <= n; ++j)
+            for (I k = 1; k <= n; ++k)
+                for (I l = 1; l <= n; ++l)
+                    atwo[(i - 1) + n * ((j - 1) + n * ((k - 1) + n * (l - 1)))] =
+                        o_ai(chol, nchovec, i + ncore, j + ncore, k + ncore, l + ncore);
+}
+
+#define ATWO(i, j, k, l) atwo[((i)-1) + n * (((j)-1) + n * (((k)-1) + n * ((l)-1)))]
+#define OUT3(arr, s, a, b) arr[((s)-1) + M * (((a)-1) + n * ((b)-1))]
+#define OUT5(arr, s, a, b, cc, d) arr[((s)-1) + M * (((a)-1) + n * (((b)-1) + n * (((cc)-1) + n * ((d)-1))))]
+#define OUT7(arr, s, a, b, cc, d, e, g)                                                              \
+    arr[((s)-1) + M * (((a)-1) + n * (((b)-1) + n * (((cc)-1) + n * (((d)-1) + n * (((e)-1) + n * ((g)-1))))))]
+#define FIDX(i, j) (o_indice((i), (j)) - 1)
+
+/* One-electron operator builders that every Koopmans routine runs first
+ * (quirk: each one overwrites the active upper triangle of f in place).
+ * mode 0: f = aj; mode 1: f = aj - 1/2 sum_c atwo(a,c,c,b); mode 2: f = aj - sum_c atwo(a,c,c,b). */
+static void o_build_f(double *f, const double *aj, const double *atwo, I n, I ncore, int mode) {
+    for (I a = 1; a <= n; ++a)
+        for (I b = a; b <= n; ++b) {
+            I jab = FIDX(a + ncore, b + ncore);
+            f[jab] = aj[jab];
+            if (mode == 0) continue;
+            for (I c = 1; c <= n; ++c) {
+                double dum = ATWO(a, c, c, b);
+                if (mode == 1) f[jab] = f[jab] - dum * 0.5;
+                else f[jab] = f[jab] - dum;
+            }
+        }
+}
+
+/* koop_matrices.F90:165-250 koopE */
+static void o_koopE(const orc_ctx *c, const double *atwo, double *koopipa, double *koopeaa, I ncore, double *f,
+                    const double *aj) {
+    I n = c->n, M = c->M;
+    o_build_f(f, aj, atwo, n, ncore, 0);
+    double *dumm = (double *)malloc(sizeof(double) * M);
+    for (I a = 1; a <= n; ++a) {
+        I ac = a + ncore;
+        for (I ap = 1; ap <= n; ++ap) {
+            for (I s = 1; s <= M; ++s) { OUT3(koopipa, s, ap, a) = 0.0; OUT3(koopeaa, s, ap, a) = 0.0; }
+            for (I cc = 1; cc <= n; ++cc) {
+                I irind = FIDX(ac, cc + ncore);
+                double dum = f[irind];
+                for (I s = 1; s <= M; ++s) OUT3(koopipa, s, ap, a) -= dum * D1(c, s, ap, cc);
+                for (I d = 1; d <= n; ++d)
+                    for (I ie = 1; ie <= n; ++ie)
+                        for (I s = 1; s <= M; ++s)
+                            OUT3(koopipa, s, ap, a) -= ATWO(cc, ie, a, d) * D2(c, s, ap, cc, d, ie);
+            }
+            for (I s = 1; s <= M; ++s) OUT3(koopipa, s, ap, a) = 2.0 * OUT3(koopipa, s, ap, a);
+        }
+    }
+    for (I ap = 1; ap <= n; ++ap)
+        for (I a = 1; a <= n; ++a) {
+            I ind = FIDX(ap + ncore, a + ncore);
+            for (I s = 1; s <= M; ++s) dumm[s - 1] = 2.0 * f[ind];
+            for (I d = 1; d <= n; ++d)
+                for (I ie = 1; ie <= n; ++ie) {
+                    double dum2 = 2.0 * ATWO(d, ie, ap, a) - ATWO(ap, ie, d, a);
+                    for (I s = 1; s <= M; ++s) dumm[s - 1] += dum2 * D1(c, s, d, ie);
+                }
+            for (I s = 1; s <= M; ++s) OUT3(koopeaa, s, ap, a) = OUT3(koopipa, s, ap, a) + 2.0 * dumm[s - 1];
+        }
+    free(dumm);
+}
+
+/* koop_matrices.F90:253-386 koop2E (C1: the its() screen is always 1). */
+static void o_koop2E(const orc_ctx *c, const double *atwo, double *koopaa, double *koopeaa, I ncore, double *f,
+                     const double *aj) {
+    I n = c->n, M = c->M;
+    o_build_f(f, aj, atwo, n, ncore, 1);
+#pragma omp parallel for collapse(2) schedule(static)
+    for (I a = 1; a <= n; ++a)
+        for (I b = 1; b <= n; ++b)
+            for (I ap = 1; ap <= n; ++ap)
+                for (I bp = 1; bp <= n; ++bp) {
+                    for (I s = 1; s <= M; ++s) OUT5(koopaa, s, ap, bp, a, b) = 0.0;
+                    for (I d = 1; d <= n; ++d) {
+                        I jad = FIDX(a + ncore, d + ncore), jbd = FIDX(b + ncore, d + ncore);
+                        for (I s = 1; s <= M; ++s)
+                            OUT5(koopaa, s, ap, bp, a, b) = OUT5(koopaa, s, ap, bp, a, b) -
+                                                            f[jad] * D2(c, s, ap, bp, d, b) -
+                                                            f[jbd] * D2(c, s, ap, bp, a, d);
+                        for (I ie = 1; ie <= n; ++ie)
+                            for (I ief = 1; ief <= n; ++ief) {
+                                double dint = ATWO(d, ie, a, ief), dint2 = ATWO(d, ie, b, ief);
+                                for (I s = 1; s <= M; ++s) {
+                                    double dum = D3(c, s, ap, bp, d, ief, b, ie);
+                                    if (d == ief) dum += 0.5 * D2(c, s, ap, bp, ie, b);
+                                    if (d == b) dum += 0.5 * D2(c, s, ap, bp, ief, ie);
+                                    OUT5(koopaa, s, ap, bp, a, b) -= dint * dum;
+                                    dum = D3(c, s, ap, bp, d, a, ief, ie);
+                                    if (d == a) dum += 0.5 * D2(c, s, ap, bp, ie, ief);
+                                    if (d == ief) dum += 0.5 * D2(c, s, ap, bp, a, ie);
+                                    OUT5(koopaa, s, ap, bp, a, b) -= dint2 * dum;
+                                }
+                            }
+                    }
+                }
+#pragma omp parallel for collapse(2) schedule(static)
+    for (I a = 1; a <= n; ++a)
+        for (I b = 1; b <= n; ++b)
+            for (I ap = 1; ap <= n; ++ap)
+                for (I bp = 1; bp <= n; ++bp) {
+                    for (I s = 1; s <= M; ++s) OUT5(koopeaa, s, ap, bp, a, b) = 0.0;
+                    for (I cc = 1; cc <= n; ++cc) {
+                        I jac = FIDX(a + ncore, cc + ncore), jbc = FIDX(b + ncore, cc + ncore);
+                        for (I s = 1; s <= M; ++s) {
+                            double dum1 = o_ro2t(c, ap, bp, cc, b, s);
+                            double dum2 = o_ro2t(c, ap, bp, a, cc, s);
+                            OUT5(koopeaa, s, ap, bp, a, b) += f[jac] * dum1 + f[jbc] * dum2;
+                        }
+                        for (I d = 1; d <= n; ++d)
+                            for (I ie = 1; ie <= n; ++ie) {
+                                double dint = ATWO(cc, ie, d, a);
+                                for (I s = 1; s <= M; ++s) {
+                                    double dum = -o_ro3t(c, ap, bp, ie, d, b, cc, s);
+                                    if (cc == ie) dum += 2.0 * o_ro2t(c, ap, bp, d, b, s);
+                                    if (d == ie) dum -= 0.5 * o_ro2t(c, ap, bp, cc, b, s);
+                                    if (b == ie) dum -= 0.5 * o_ro2t(c, ap, bp, d, cc, s);
+                                    OUT5(koopeaa, s, ap, bp, a, b) += dint * dum;
+                                }
+                                dint = ATWO(cc, ie, d, b);
+                                for (I s = 1; s <= M; ++s) {
+                                    double dum = -o_ro3t(c, ap, bp, ie, a, d, cc, s);
+                                    if (cc == ie) dum += 2.0 * o_ro2t(c, ap, bp, a, d, s);
+                                    if (a == ie) dum -= 0.5 * o_ro2t(c, ap, bp, cc, d, s);
+                                    if (d == ie) dum -= 0.5 * o_ro2t(c, ap, bp, a, cc, s);
+                                    OUT5(koopeaa, s, ap, bp, a, b) += dint * dum;
+                                }
+                            }
+                    }
+                }
+}
+
+/* koop_matrices.F90:389-588 koopman0pE */
+static void o_koopman0pE(const orc_ctx *c, const double *atwo, double *koopaa, double *koopbb, double *koopab,
+                         I ncore, double *f, const double *aj) {
+    I n = c->n, M = c->M;
+    o_build_f(f, aj, atwo, n, ncore, 1);
+#pragma omp parallel for collapse(2) schedule(static)
+    for (I a = 1; a <= n; ++a)
+        for (I b = 1; b <= n; ++b) {
+            I ac = a + ncore, bc = b + ncore;
+            for (I ap = 1; ap <= n; ++ap)
+                for (I bp = 1; bp <= n; ++bp) {
+                    for (I s = 1; s <= M; ++s) OUT5(koopaa, s, bp, ap, a, b) = 0.0;
+                    for (I cc = 1; cc <= n; ++cc) {
+                        I ica = FIDX(cc + ncore, ac), ibc = FIDX(bc, cc + ncore);
+                        for (I s = 1; s <= M; ++s)
+                            OUT5(koopaa, s, bp, ap, a, b) += 2.0 * (f[ica] * o_ee2(c, bp, ap, cc, b, s) -
+                                                                    f[ibc] * o_ee2(c, bp, ap, a, cc, s));
+                        for (I d = 1; d <= n; ++d)
+                            for (I ie = 1; ie <= n; ++ie)
+                                for (I s = 1; s <= M; ++s) {
+                                    double dum1 = o_eee2(c, bp, ap, cc, ie, d, b, s) + o_eee2(c, bp, ap, d, b, cc, ie, s);
+                                    double dum2 = o_eee2(c, bp, ap, a, ie, cc, d, s) + o_eee2(c, bp, ap, cc, d, a, ie, s);
+                                    OUT5(koopaa, s, bp, ap, a, b) += ATWO(cc, ie, d, a) * dum1 - ATWO(b, ie, cc, d) * dum2;
+                                }
+                    }
+                    for (I s = 1; s <= M; ++s) OUT5(koopbb, s, bp, ap, a, b) = 0.0;
+                    for (I cc = 1; cc <= n; ++cc) {
+                        I ica = FIDX(cc + ncore, ac), ibc = FIDX(bc, cc + ncore);
+                        for (I s = 1; s <= M; ++s) {
+                            double dum1 = -o_ee2(c, a, ap, bp, cc, s);
+                            if (a == ap) dum1 += 2.0 * D1(c, s, bp, cc);
+                            if (bp == ap) dum1 += D1(c, s, a, cc);
+                            double dum2 = -o_ee2(c, cc, ap, bp, b, s);
+                            if (ap == cc) dum2 += 2.0 * D1(c, s, bp, b);
+                            if (bp == ap) dum2 += D1(c, s, cc, b);
+                            OUT5(koopbb, s, bp, ap, a, b) += -f[ibc] * dum1 + f[ica] * dum2;
+                        }
+                        for (I d = 1; d <= n; ++d)
+                            for (I ie = 1; ie <= n; ++ie)
+                                for (I s = 1; s <= M; ++s) {
+                                    double dum1 = -o_eee2(c, cc, ie, a, ap, bp, d, s) - o_eee2(c, a, ap, bp, d, cc, ie, s);
+                                    if (ap == a) dum1 += 2.0 * (o_ee2(c, cc, ie, bp, d, s) + o_ee2(c, bp, d, cc, ie, s));
+                                    if (bp == ap) dum1 += o_ee2(c, cc, ie, a, d, s) + o_ee2(c, a, d, cc, ie, s);
+                                    if (ap == cc) {
+                                        dum1 -= o_ee2(c, a, ie, bp, d, s);
+                                        if (ie == a) dum1 += 2.0 * D1(c, s, bp, d);
+                                    }
+                                    if (bp == ie) {
+                                        dum1 += o_ee2(c, a, ap, cc, d, s);
+                                        if (ap == a) dum1 -= 2.0 * D1(c, s, cc, d);
+                                    }
+                                    double dum2 = -o_eee2(c, cc, ie, d, ap, bp, b, s) - o_eee2(c, d, ap, bp, b, cc, ie, s);
+                                    if (ap == d) dum2 += 2.0 * (o_ee2(c, cc, ie, bp, b, s) + o_ee2(c, bp, b, cc, ie, s));
+                                    if (bp == ap) dum2 += o_ee2(c, cc, ie, d, b, s) + o_ee2(c, d, b, cc, ie, s);
+                                    if (ap == cc) {
+                                        dum2 -= o_ee2(c, d, ie, bp, b, s);
+                                        if (d == ie) dum2 += 2.0 * D1(c, s, bp, b);
+                                    }
+                                    if (bp == ie) {
+                                        dum2 += o_ee2(c, d, ap, cc, b, s);
+                                        if (d == ap) dum2 -= 2.0 * D1(c, s, cc, b);
+                                    }
+                                    OUT5(koopbb, s, bp, ap, a, b) += -0.5 * ATWO(cc, ie, b, d) * dum1 + 0.5 * ATWO(cc, ie, d, a) * dum2;
+                                }
+                    }
+                }
+            for (I s = 1; s <= M; ++s) OUT3(koopab, s, a, b) = 0.0;
+            for (I cc = 1; cc <= n; ++cc) {
+                I ica = FIDX(cc + ncore, ac), ibc = FIDX(bc, cc + ncore);
+                for (I s = 1; s <= M; ++s) {
+                    double dum1 = D1(c, s, cc, b), dum2 = D1(c, s, a, cc);
+                    OUT3(koopab, s, a, b) += 2.0 * (f[ica] * dum1 - f[ibc] * dum2);
+                }
+                for (I d = 1; d <= n; ++d)
+                    for (I ie = 1; ie <= n; ++ie)
+                        for (I s = 1; s <= M; ++s) {
+                            double dum1 = o_ee2(c, cc, ie, d, b, s) + o_ee2(c, d, b, cc, ie, s);
+                            double dum2 = o_ee2(c, a, ie, cc, d, s) + o_ee2(c, cc, d, a, ie, s);
+                            OUT3(koopab, s, a, b) += ATWO(cc, ie, d, a) * dum1 - ATWO(b, ie, cc, d) * dum2;
+                        }
+            }
+        }
+}
+
+/* koop_matrices.F90:16-31 koop_matrices_ctl.  The reference writes these to
+ * nevpt.h5; here they come back as buffers:
+ *   ipko1,eako1 (M,n,n) "1-IPKO","1-EAKO"; hrdm2 (M,n^4) "2-HRDM";
+ *   ipko2 (M,n^4) "2-IPKO" (the 2-HRDM buffer is overwritten by koop2E in the
+ *   reference, so "2-HRDM" is snapshotted before); eako2 "2-EAKO";
+ *   gk0pa, gk0pd (M,n^4); gk0pf (M,n,n).  f is the in/out scratch. */
+void orc_koop_matrices_ctl(I metat, I nact, I ncore, const double *atwo, const double *daaa, const double *taa,
+                           const double *dal, double *f, const double *aj, double *ipko1, double *eako1,
+                           double *hrdm2, double *ipko2, double *eako2, double *gk0pa, double *gk0pd,
+                           double *gk0pf) {
+    orc_ctx c;
+    memset(&c, 0, sizeof c);
+    c.n = nact; c.M = metat; c.d1 = dal; c.d2 = taa; c.d3 = daaa;
+    I n = nact, M = metat;
+    o_koopE(&c, atwo, ipko1, eako1, ncore, f, aj);
+    for (I i = 1; i <= n; ++i)
+        for (I j = 1; j <= n; ++j)
+            for (I k = 1; k <= n; ++k)
+                for (I l = 1; l <= n; ++l)
+                    for (I s = 1; s <= M; ++s) OUT5(hrdm2, s, i, j, k, l) = o_ro2t(&c, i, j, k, l, s);
+    /* koop2E overwrites koopaa (which held the 2-HRDM) with the 2-IP matrix. */
+    memcpy(ipko2, hrdm2, sizeof(double) * (size_t)(M * n * n * n * n));
+    o_koop2E(&c, atwo, ipko2, eako2, ncore, f, aj);
+    /* koopman0pE reuses the koopaa buffer: it fully overwrites it (gk0pa). */
+    o_koopman0pE(&c, atwo, gk0pa, gk0pd, gk0pf, ncore, f, aj);
+}
+
+/* koop_matrices.F90:591-619 fdiff_F: per state max |F|. */
+void orc_fdiff_F(const double *koopab, I nact, I metat, double *maxabs) {
+    I n = nact, M = metat;
+    for (I s = 1; s <= M; ++s) {
+        double big = 0.0;
+        for (I i = 1; i <= n; ++i)
+            for (I j = 1; j <= n; ++j) {
+                double v = fabs(OUT3(koopab, s, i, j));
+                if (v > big) big = v;
+            }
+        maxabs[s - 1] = big;
+    }
+}
+
+/* koopro4QD.F90:3974-4104 bamat, C1 branch.  The reference loops (a,b,c,ap,bp,cp)
+ * and scatters the "transposed" EA terms into atmat(ap,b,cp,a,bp,c) under OpenMP
+ * atomics; here the outer (a,c) pair is split across threads, which keeps every
+ * write of one iteration inside the thread that owns (a,c). */
+static void o_bamat_range(double *amat, double *atmat, const double *atwo, const double *ro4, const double *daaa,
+                          const double *taa, const double *dal, I nact, I ncore, double *f, const double *aj,
+                          I metat, I slab_lo, I slab_hi) {
+    orc_ctx c;
+    o_init(&c, nact, metat);
+    c.d1 = dal; c.d2 = taa; c.d3 = daaa; c.ro4 = ro4;
+    I n = nact, M = metat;
+    o_build_f(f, aj, atwo, n, ncore, 1);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (I slab = slab_lo; slab < slab_hi; ++slab)
+            for (I b = 1; b <= n; ++b) {
+                I a = slab / n + 1, cc = slab % n + 1;
+                for (I ap = 1; ap <= n; ++ap)
+                    for (I bp = 1; bp <= n; ++bp)
+                        for (I cp = 1; cp <= n; ++cp)
+                            for (I d = 1; d <= n; ++d) {
+                                double fda = f[FIDX(d + ncore, a + ncore)];
+                                double fcd = f[FIDX(cc + ncore, d + ncore)];
+                                double fbd = f[FIDX(b + ncore, d + ncore)];
+                                for (I s = 1; s <= M; ++s) {
+                                    OUT7(amat, s, ap, bp, cp, a, b, cc) += fda * o_eee2(&c, cp, ap, bp, b, d, cc, s) -
+                                                                          fcd * o_eee2(&c, cp, ap, bp, b, a, d, s) -
+                                                                          fbd * o_eee2(&c, cp, ap, bp, d, a, cc, s);
+                                    OUT7(atmat, s, ap, bp, cp, a, b, cc) += fda * o_eee2t(&c, cp, ap, bp, b, d, cc, s) -
+                                                                           fcd * o_eee2t(&c, cp, ap, bp, b, a, d, s) +
+                                                                           fbd * o_eee2t(&c, cp, ap, bp, d, a, cc, s);
+                                }
+                                for (I ie = 1; ie <= n; ++ie) {
+                                    double dint1 = ATWO(cc, ie, d, a), dint2 = ATWO(d, ie, ie, a);
+                                    double dint3 = ATWO(cc, d, d, ie), dint4 = ATWO(b, d, d, ie);
+                                    for (I s = 1; s <= M; ++s) {
+                                        double dum1 = o_eee2(&c, cp, ap, bp, b, d, ie, s);
+                                        double dum2 = o_eee2(&c, cp, ap, bp, b, d, cc, s);
+                                        double dum3 = o_eee2(&c, cp, ap, bp, b, a, ie, s);
+                                        double dum4 = o_eee2(&c, cp, ap, bp, ie, a, cc, s);
+                                        double dum1t = -dum1, dum2t = -dum2, dum3t = -dum3;
+                                        if (bp == b) {
+                                            dum1t += 2.0 * o_ee2(&c, cp, ap, d, ie, s);
+                                            dum2t += 2.0 * o_ee2(&c, cp, ap, d, cc, s);
+                                            dum3t += 2.0 * o_ee2(&c, cp, ap, a, ie, s);
+                                        }
+                                        OUT7(atmat, s, ap, b, cp, a, bp, cc) += dum1t * dint1 - 0.5 * (dum2t * dint2 + dum3t * dint3);
+                                        double dum4t = o_eee2t(&c, cp, ap, bp, ie, a, cc, s);
+                                        OUT7(amat, s, ap, bp, cp, a, b, cc) += dum1 * dint1 - 0.5 * (dum2 * dint2 + dum3 * dint3 - dum4 * dint4);
+                                        OUT7(atmat, s, ap, bp, cp, a, b, cc) += 0.5 * dum4t * dint4;
+                                    }
+                                    for (I ief = 1; ief <= n; ++ief)
+                                        for (I s = 1; s <= M; ++s) {
+                                            double di1 = ATWO(d, ief, ie, a);
+                                            double e1 = o_eeee(&c, cp, ap, bp, b, d, ief, ie, cc, s);
+                                            double e1t = -e1;
+                                            if (bp == b) e1t += 2.0 * o_eee2(&c, cp, ap, d, ief, ie, cc, s);
+                                            OUT7(amat, s, ap, bp, cp, a, b, cc) += e1 * di1;
+                                            OUT7(atmat, s, ap, b, cp, a, bp, cc) += e1t * di1;
+                                            double e2 = o_eeee(&c, cp, ap, bp, b, d, ief, a, ie, s);
+                                            double e2t = -e2;
+                                            if (bp == b) e2t += 2.0 * o_eee2(&c, cp, ap, d, ief, a, ie, s);
+                                            double di2 = ATWO(d, ief, cc, ie);
+                                            OUT7(amat, s, ap, bp, cp, a, b, cc) -= e2 * di2;
+                                            OUT7(atmat, s, ap, b, cp, a, bp, cc) -= e2t * di2;
+                                            double e3 = o_eeee(&c, cp, ap, bp, ie, d, ief, a, cc, s);
+                                            double e3t = o_eeeet(&c, cp, ap, bp, ie, d, ief, a, cc, s);
+                                            double di3 = ATWO(d, ief, b, ie);
+                                            OUT7(amat, s, ap, bp, cp, a, b, cc) -= e3 * di3;
+                                            OUT7(atmat, s, ap, bp, cp, a, b, cc) += e3t * di3;
+                                        }
+                                }
+                            }
+            }
+    o_free(&c);
+}
+
+void orc_bamat(double *amat, double *atmat, const double *atwo, const double *ro4, const double *daaa,
+               const double *taa, const double *dal, I nact, I ncore, double *f, const double *aj, I norb,
+               I metat) {
+    (void)norb;
+    o_bamat_range(amat, atmat, atwo, ro4, daaa, taa, dal, nact, ncore, f, aj, metat, 0, nact * nact);
+}
+
+/* Time-bounded variant for the CPU baseline: runs the bamat iterations of the
+ * first `nslab` (a,c) slabs only (each slab is 1/n^2 of the work).  Output
+ * values are partial; only the timing is used. */
+void orc_bamat_slabs(double *amat, double *atmat, const double *atwo, const double *ro4, const double *daaa,
+                     const double *taa, const double *dal, I nact, I ncore, double *f, const double *aj, I metat,
+                     I nslab) {
+    if (nslab > nact * nact) nslab = nact * nact;
+    o_bamat_range(amat, atmat, atwo, ro4, daaa, taa, dal, nact, ncore, f, aj, metat, 0, nslab);
+}
+
+/* koopro4QD.F90:4231-4299 bbmat (quirk: the EA part multiplies by aj, not f). */
+void orc_bbmat(const double *atwo, double *bmat, double *btmat, const double *daaa, const double *taa,
+               const double *dal, I nact, I ncore, double *f, const double *aj, I metat) {
+    orc_ctx c;
+    memset(&c, 0, sizeof c);
+    c.n = nact; c.M = metat; c.d1 = dal; c.d2 = taa; c.d3 = daaa;
+    I n = nact, M = metat;
+    o_build_f(f, aj, atwo, n, ncore, 2);
+#pragma omp parallel for collapse(2) schedule(static)
+    for (I ap = 1; ap <= n; ++ap)
+        for (I bp = 1; bp <= n; ++bp)
+            for (I cp = 1; cp <= n; ++cp)
+                for (I a = 1; a <= n; ++a) {
+                    I ac = a + ncore;
+                    for (I s = 1; s <= M; ++s) { OUT5(bmat, s, ap, bp, cp, a) = 0.0; OUT5(btmat, s, ap, bp, cp, a) = 0.0; }
+                    for (I cc = 1; cc <= n; ++cc) {
+                        I iac = FIDX(cc + ncore, ac);
+                        for (I s = 1; s <= M; ++s) {
+                            OUT5(bmat, s, ap, bp, cp, a) -= f[iac] * o_ee2(&c, cp, ap, bp, cc, s);
+                            OUT5(btmat, s, ap, bp, cp, a) += aj[iac] * o_ee2tr(&c, cp, ap, bp, cc, s);
+                        }
+                        for (I ie = 1; ie <= n; ++ie)
+                            for (I ief = 1; ief <= n; ++ief) {
+                                double dint = ATWO(a, ie, cc, ief);
+                                for (I s = 1; s <= M; ++s) {
+                                    double dum = o_eee2(&c, cp, ap, bp, ie, cc, ief, s);
+                                    double dumt = o_eee2t(&c, cp, ap, bp, ie, cc, ief, s);
+                                    OUT5(bmat, s, ap, bp, cp, a) -= dum * dint;
+                                    OUT5(btmat, s, ap, bp, cp, a) += dumt * dint;
+                                }
+                            }
+                    }
+                }
+}
+
+/* koopro4QD.F90:4301-4397 bcmat.  The reference's (ap,a,b,c,d) loop nest
+ * accumulates into cmat(ap,a,b,c) with atomics; the d loop is the reduction,
+ * so the parallel split is over (ap,a). */
+void orc_bcmat(const double *atwo, double *cmat, double *ctmat, const double *daaa, const double *taa,
+               const double *dal, I nact, I ncore, double *f, const double *aj, I metat) {
+    orc_ctx c;
+    memset(&c, 0, sizeof c);
+    c.n = nact; c.M = metat; c.d1 = dal; c.d2 = taa; c.d3 = daaa;
+    I n = nact, M = metat;
+    o_build_f(f, aj, atwo, n, ncore, 1);
+    memset(cmat, 0, sizeof(double) * (size_t)(M * n * n * n * n));
+    memset(ctmat, 0, sizeof(double) * (size_t)(M * n * n * n * n));
+#pragma omp parallel for collapse(2) schedule(static)
+    for (I ap = 1; ap <= n; ++ap)
+        for (I a = 1; a <= n; ++a)
+            for (I b = 1; b <= n; ++b)
+                for (I cc = 1; cc <= n; ++cc)
+                    for (I d = 1; d <= n; ++d) {
+                        I ida = FIDX(d + ncore, a + ncore), icd = FIDX(cc + ncore, d + ncore), ibd = FIDX(b + ncore, d + ncore);
+                        for (I s = 1; s <= M; ++s) {
+                            OUT5(cmat, s, ap, a, b, cc) += f[ida] * o_ee2(&c, ap, b, d, cc, s) -
+                                                           f[icd] * o_ee2(&c, ap, b, a, d, s) -
+                                                           f[ibd] * o_ee2(&c, ap, d, a, cc, s);
+                            OUT5(ctmat, s, ap, a, b, cc) += f[ida] * o_ee2t(&c, ap, b, d, cc, s) -
+                                                            f[icd] * o_ee2t(&c, ap, b, a, d, s) +
+                                                            f[ibd] * o_ee2t(&c, ap, d, a, cc, s);
+                        }
+                        for (I ie = 1; ie <= n; ++ie) {
+                            double dint1 = ATWO(cc, ie, d, a), dint2 = ATWO(d, ie, ie, a);
+                            double dint3 = ATWO(cc, d, d, ie), dint4 = ATWO(b, d, d, ie);
+                            for (I s = 1; s <= M; ++s) {
+                                double dum1 = o_ee2(&c, ap, b, d, ie, s), dum2 = o_ee2(&c, ap, b, d, cc, s);
+                                double dum3 = o_ee2(&c, ap, b, a, ie, s), dum4 = o_ee2(&c, ap, ie, a, cc, s);
+                                double dum1t = o_ee2t(&c, ap, b, d, ie, s), dum2t = o_ee2t(&c, ap, b, d, cc, s);
+                                double dum3t = o_ee2t(&c, ap, b, a, ie, s), dum4t = o_ee2t(&c, ap, ie, a, cc, s);
+                                OUT5(cmat, s, ap, a, b, cc) += dum1 * dint1 - 0.5 * (dum2 * dint2 + dum3 * dint3 - dum4 * dint4);
+                                OUT5(ctmat, s, ap, a, b, cc) += dum1t * dint1 - 0.5 * (dum2t * dint2 + dum3t * dint3 - dum4t * dint4);
+                            }
+                            for (I ief = 1; ief <= n; ++ief) {
+                                double di1 = ATWO(d, ief, ie, a), di2 = ATWO(d, ief, cc, ie), di3 = ATWO(d, ief, b, ie);
+                                for (I s = 1; s <= M; ++s) {
+                                    double e1 = o_eee2(&c, ap, b, d, ief, ie, cc, s);
+                                    double e1t = o_eee2tl(&c, ap, b, d, ief, ie, cc, s);
+                                    double e2 = o_eee2(&c, ap, b, d, ief, a, ie, s);
+                                    double e2t = o_eee2tl(&c, ap, b, d, ief, a, ie, s);
+                                    double e3 = o_eee2(&c, ap, ie, d, ief, a, cc, s);
+                                    double e3t = o_eee2tl(&c, ap, ie, d, ief, a, cc, s);
+                                    OUT5(cmat, s, ap, a, b, cc) += e1 * di1 - e2 * di2 - e3 * di3;
+                                    OUT5(ctmat, s, ap, a, b, cc) += e1t * di1 - e2t * di2 + e3t * di3;
+                                }
+                            }
+                        }
+                    }
+}
+
+/* koopro4QD.F90:4399-4459 bdmat (quirk: the EA part multiplies by aj). */
+void orc_bdmat(const double *atwo, double *dmat, double *dtmat, const double *taa, const double *dal, I nact,
+               I ncore, double *f, const double *aj, I metat) {
+    orc_ctx c;
+    memset(&c, 0, sizeof c);
+    c.n = nact; c.M = metat; c.d1 = dal; c.d2 = taa;
+    I n = nact, M = metat;
+    o_build_f(f, aj, atwo, n, ncore, 2);
+    for (I ap = 1; ap <= n; ++ap)
+        for (I a = 1; a <= n; ++a) {
+            I ac = a + ncore;
+            for (I s = 1; s <= M; ++s) { OUT3(dmat, s, ap, a) = 0.0; OUT3(dtmat, s, ap, a) = 0.0; }
+            for (I cc = 1; cc <= n; ++cc) {
+                I iac = FIDX(cc + ncore, ac);
+                for (I s = 1; s <= M; ++s) {
+                    OUT3(dmat, s, ap, a) -= f[iac] * D1(&c, s, ap, cc);
+                    double dum = -D1(&c, s, ap, cc);
+                    if (ap == cc) dum += 2.0;
+                    OUT3(dtmat, s, ap, a) += aj[iac] * dum;
+                }
+                for (I ie = 1; ie <= n; ++ie)
+                    for (I ief = 1; ief <= n; ++ief) {
+                        double dint = ATWO(a, ie, cc, ief);
+                        for (I s = 1; s <= M; ++s) {
+                            double dum = o_ee2(&c, ap, ie, cc, ief, s);
+                            double dumt = o_ee2t(&c, ap, ie, cc, ief, s);
+                            OUT3(dmat, s, ap, a) -= dum * dint;
+                            OUT3(dtmat, s, ap, a) += dumt * dint;
+                        }
+                    }
+            }
+        }
+}
+
+/* koopro4QD.F90:5053-5112 fdiff: per state max |B(i,j,ii,jj) - C(jj,i,j,ii)|
+ * for the IP pair (out[0..M)) and the EA pair (out[M..2M)). */
+void orc_fdiff(const double *bmat, const double *cmat, const double *btmat, const double *ctmat, I nact, I metat,
+               double *out) {
+    I n = nact, M = metat;
+    for (int which = 0; which < 2; ++which) {
+        const double *B = which ? btmat : bmat, *C = which ? ctmat : cmat;
+        for (I s = 1; s <= M; ++s) {
+            double big = 0.0;
+            for (I i = 1; i <= n; ++i)
+                for (I j = 1; j <= n; ++j)
+                    for (I ii = 1; ii <= n; ++ii)
+                        for (I jj = 1; jj <= n; ++jj) {
+                            double d = fabs(OUT5(B, s, i, j, ii, jj) - OUT5(C, s, jj, i, j, ii));
+                            if (d > big) big = d;
+                        }
+            out[which * M + s - 1] = big;
+        }
+    }
+}
+
+/* Direct accessor entry points for tests of the inner formulas. */
+double orc_eeee_at(const double *ro4, const double *daaa, const double *taa, const double *dal, I nact, I metat,
+                   const I *idx8, I s) {
+    orc_ctx c;
+    o_init(&c, nact, metat);
+    c.d1 = dal; c.d2 = taa; c.d3 = daaa; c.ro4 = ro4;
+    double r = o_eeee(&c, idx8[0], idx8[1], idx8[2], idx8[3], idx8[4], idx8[5], idx8[6], idx8[7], s);
+    o_free(&c);
+    return r;
+}
+
+double orc_eee2_at(const double *daaa, const double *taa, const double *dal, I nact, I metat, const I *idx6, I s) {
+    orc_ctx c;
+    memset(&c, 0, sizeof c);
+    c.n = nact; c.M = metat; c.d1 = dal; c.d2 = taa; c.d3 = daaa;
+    return o_eee2(&c, idx6[0], idx6[1], idx6[2], idx6[3], idx6[4], idx6[5], s);
+}
+
+int orc_num_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
