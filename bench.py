@@ -1,0 +1,299 @@
+"""Benchmark: seconds per state of the Koopmans + NEVPT2 path on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step is one pass of the hot path over one problem (all of its states), on
+a seeded synthetic CAS(14,14) problem: 50,000 determinants drawn uniformly
+from CAS(14,14) with 7 alpha + 7 beta electrons, Gaussian coefficients, 20
+inactive and 150 virtual orbitals, density-fitted integrals with 4*norb
+vectors.  The packed 4-RDM (0.73 GB) is larger than L2, and L2 is flushed
+between timed steps as well.
+
+value: device time per state with every input resident in HBM (CUDA events
+on the launching stream).  e2e: the same metric through the public host API
+(koopro.koopro4QD with pinned host arrays), host<->device copies included.
+Multi-GPU: the path shards over states and independent problems, so N ranks
+run N replicas (weak scaling) with no collective on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "s/state for Koopmans+SC/PC-NEVPT2 at CAS(16,16); split vs FP64 at ≤1e-7 Eh"
+WORKLOAD = "cas14"
+
+
+def _args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default=WORKLOAD)
+    ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the bounded CPU baseline sample")
+    return ap.parse_args()
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+def workload_desc(p):
+    return {"workload": f"CAS({p.nact},{p.nele}) {p.ndet} determinants, {p.ncore} inactive / {p.nvirt} virtual, "
+                        f"{p.metat} state(s), DF integrals Q={p.nchovec}",
+            "nact": p.nact, "nele": p.nele, "ncore": p.ncore, "nvirt": p.nvirt, "states": p.metat,
+            "determinants": p.ndet, "precision": "fp64",
+            "scope": "stage 1 (Koopmans matrices: bro3/bro2/bro1, get_aj_atwo, koop_matrices_ctl, bamat, bbmat, "
+                     "bcmat, bdmat); stage 2 (SC/PC classes) not yet on the device",
+            "l2": "inputs larger than L2 (packed 4-RDM) and a 512 MB L2 flush between timed steps"}
+
+
+class Clocks:
+    """Samples nvidia-smi during the timed region."""
+
+    def __init__(self):
+        self.samples = []
+        self._stop = threading.Event()
+        self._proc = None
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self._proc = subprocess.Popen(["nvidia-smi", "-i", os.environ.get("LOCAL_RANK", "0"),
+                                           f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "200"],
+                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except FileNotFoundError:
+            self._proc = None
+            return
+        threading.Thread(target=self._read, daemon=True).start()
+
+    def _read(self):
+        for line in self._proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self._proc:
+            self._proc.terminate()
+            try:
+                self._proc.wait(2)
+            except Exception:
+                self._proc.kill()
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].strip() == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def cpu_baseline(p, budget_s: float):
+    """Times the CPU oracle (C restatement, OpenMP over all host threads) on a
+    bounded sample: the full n^5-n^7 Koopmans builders plus `k` of the n^2
+    (a,c) slabs of the n^9 A-matrix builder, extrapolated to the whole stage."""
+    from oracle import oracle as orc
+
+    n, nc, M = p.nact, p.ncore, p.metat
+    t0 = time.perf_counter()
+    atwo, aj = orc.get_aj_atwo(p.oneint, p.chol, n, nc, p.norb)
+    f = np.zeros(p.norb * (p.norb + 1) // 2)
+    orc.koop_matrices_ctl(M, n, nc, atwo, p.daaa, p.taa, p.dal, f, aj)
+    orc.bbmat(atwo, p.daaa, p.taa, p.dal, n, nc, f, aj, M)
+    orc.bcmat(atwo, p.daaa, p.taa, p.dal, n, nc, f, aj, M)
+    orc.bdmat(atwo, p.taa, p.dal, n, nc, f, aj, M)
+    d3 = orc.bro3(p.ro4, n, p.nele, M)
+    t_rest = time.perf_counter() - t0
+    threads = orc.num_threads()
+    k = 1
+    t1 = time.perf_counter()
+    orc.bamat_slabs(atwo, p.ro4, p.daaa, p.taa, p.dal, n, nc, f, aj, M, k * threads)
+    t_slab = (time.perf_counter() - t1) / (k * threads)
+    remaining = max(budget_s - (time.perf_counter() - t0), 0.0)
+    extra = int(min(remaining / max(t_slab, 1e-9), n * n - threads) // threads) * threads
+    if extra > 0:
+        t2 = time.perf_counter()
+        orc.bamat_slabs(atwo, p.ro4, p.daaa, p.taa, p.dal, n, nc, f, aj, M, extra)
+        t_slab = (time.perf_counter() - t2) / extra
+        k_slabs = extra
+    else:
+        k_slabs = threads
+    total = t_rest + t_slab * n * n
+    del d3
+    return {"value": total / M, "unit": "s/state", "cores": threads, "kind": "port",
+            "sample": f"C restatement of the reference loops (OpenMP, {threads} threads): every stage-1 builder "
+                      f"except bamat run in full ({t_rest:.2f} s); bamat timed on {k_slabs} of {n * n} (a,c) slabs "
+                      f"and scaled by n^2/slabs"}
+
+
+def run_reference(args):
+    ws, rank = _dist()
+    if rank != 0:
+        return
+    from nevpt2_gb300 import synth
+    p = synth.config_problem(args.config)
+    vals = []
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline(p, args.cpu_seconds)
+        if i >= args.warmup:
+            vals.append(cb["value"])
+    v = float(np.mean(vals))
+    cb["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "s/state", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * p.metat * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded CI vector, exact RDMs, random DF integrals)", "config": workload_desc(p),
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": "s/state", "h2d_bytes_per_step": 0,
+                                        "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    from nevpt2_gb300 import koopro, synth
+    from nevpt2_gb300.pipeline import Stage1
+
+    ws, rank = _dist()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if ws > 1:
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    p = synth.config_problem(args.config)
+    n, M = p.nact, p.metat
+
+    # ---------------- device-resident timing (value) ----------------
+    st = Stage1(p, device=str(dev))
+    stream = torch.cuda.Stream(dev)
+    flush = torch.empty(512 * 2**20 // 4, dtype=torch.float32, device=dev)
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            st.run(stream)
+    torch.cuda.synchronize(dev)
+    # bamat alone, for the roofline (same stream)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    clocks = Clocks()
+    clocks.start()
+    launches0 = st.ctx.launches
+    times = []
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            flush.zero_()
+            starts[i].record(stream)
+            st.run(stream)
+            ends[i].record(stream)
+    torch.cuda.synchronize(dev)
+    launches = st.ctx.launches - launches0
+    clk = clocks.stop()
+    times = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    ms = float(np.mean(times))
+    if ws > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+
+    # bamat kernel alone: CUDA events on the launching stream
+    with torch.cuda.stream(stream):
+        flush.zero_()
+        ev[0].record(stream)
+        from nevpt2_gb300._native import ptr
+        from nevpt2_gb300.pipeline import ptr_stream
+        o = st.out
+        st.ctx.call("nvpt_bamat_d", ptr(o["amatIP"]), ptr(o["amatEA"]), ptr(st.atwo), ptr(st.ro4), ptr(st.daaa),
+                    ptr(st.taa), ptr(st.dal), n, p.ncore, ptr(st.f), ptr(st.aj), p.norb, M, 1, ptr_stream(stream))
+        ev[1].record(stream)
+    torch.cuda.synchronize(dev)
+    bamat_ms = ev[0].elapsed_time(ev[1])
+
+    # ---------------- end to end through the host API (e2e) ----------------
+    pinned = {}
+    for name in ("ro4", "oneint", "chol"):
+        a = getattr(p, name)
+        t = torch.empty(a.size, dtype=torch.float64).pin_memory()
+        t.numpy()[:] = a.reshape(-1, order="F")
+        pinned[name] = t.numpy().reshape(a.shape, order="F")
+    from dataclasses import replace
+    pp = replace(p, ro4=pinned["ro4"], oneint=pinned["oneint"], chol=pinned["chol"])
+    koopro.koopro4QD(pp)  # warm
+    e2e_t = []
+    for _ in range(max(1, min(args.steps, 3))):
+        t0 = time.perf_counter()
+        res = koopro.koopro4QD(pp)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e = float(np.mean(e2e_t)) / M
+    W = p.nwords
+    b8 = 8
+    h2d = b8 * (2 * W * n**4 * M + p.oneint.size + p.chol.size + 6 * (M * n**6) + 10 * (M * n**4) + 10 * n**4)
+    d2h = b8 * sum(v.size for v in res.values())
+
+    if rank != 0:
+        dist.destroy_process_group() if ws > 1 else None
+        return
+    # roofline: bamat's algorithmic bytes per launch = 8*(live packed 4-RDM + Gamma3 + atwo + 2 outputs)
+    live = live_ro4_entries(n)
+    alg_bytes = 8 * M * (live + n**6 + 2 * n**6) + 8 * n**4
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = alg_bytes / (bamat_ms * 1e-3) / 1e9
+    cb = cpu_baseline(p, args.cpu_seconds)
+    line = {"metric": METRIC, "value": ms / 1e3 / M, "unit": "s/state", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded CI vector, exact RDMs, random DF integrals)",
+            "config": workload_desc(p), "gpu_launches": int(launches),
+            "e2e": {"value": e2e, "unit": "s/state", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "roofline": {"kernel": "k_bamat_direct", "bound": "hbm", "achieved": achieved, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback",
+                         "kernel_ms": bamat_ms, "alg_bytes": alg_bytes},
+            "clocks": clk, "cpu_baseline": cb, "step_ms_all": times}
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+def live_ro4_entries(n: int) -> int:
+    """Packed 4-RDM slots ord8 can address: (K sorted descending, L) with
+    normind(L) <= normind(K)."""
+    import itertools
+    def lind(q):
+        s = sorted(q, reverse=True)
+        return (s[0] - 1) * s[0] * (s[0] + 1) * (s[0] + 2) // 24 + (s[1] - 1) * s[1] * (s[1] + 1) // 6 + \
+            s[2] * (s[2] - 1) // 2 + s[3]
+    vals = np.array([lind(q) for q in itertools.product(range(1, n + 1), repeat=4)])
+    counts = np.bincount(vals)  # counts[v] = number of L with normind == v
+    cum = np.cumsum(counts)
+    W = n * (n + 1) * (n + 2) * (n + 3) // 24
+    return int(sum(cum[k] for k in range(1, W + 1)))
+
+
+if __name__ == "__main__":
+    a = _args()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)

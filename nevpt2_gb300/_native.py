@@ -30,11 +30,20 @@ class NvptError(RuntimeError):
 STATUS = {0: "NVPT_OK", 1: "NVPT_EINVAL", 2: "NVPT_ECUDA", 3: "NVPT_ENOMEM", 4: "NVPT_ENOTSUP", 5: "NVPT_ETIMEDOUT"}
 
 
-def header_functions() -> list[str]:
-    """Every function name include/nvpt2.h declares."""
+def header_prototypes() -> dict[str, list[str]]:
+    """Every function include/nvpt2.h declares -> its parameter types."""
     txt = HEADER.read_text()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
-    return sorted(set(re.findall(r"\b(nvpt_\w+)\s*\(", txt)))
+    out = {}
+    for m in re.finditer(r"\b(nvpt_\w+)\s*\(([^;{]*?)\)\s*;", txt, flags=re.S):
+        params = [" ".join(x.split()) for x in m.group(2).split(",") if x.strip() and x.strip() != "void"]
+        out[m.group(1)] = [re.sub(r"\s*\b\w+$", "", x) if not x.endswith("*") else x for x in params]
+    return out
+
+
+def header_functions() -> list[str]:
+    """Every function name include/nvpt2.h declares."""
+    return sorted(header_prototypes())
 
 
 _SIGS = {
@@ -50,7 +59,7 @@ _SIGS = {
     "nvpt_bro2": ([P, P, P, I64, I64, I64], ctypes.c_int),
     "nvpt_bro1": ([P, P, P, I64, I64, I64], ctypes.c_int),
     "nvpt_get_aj_atwo": ([P, P, I64, I64, I64, P, P, P, I64], ctypes.c_int),
-    "nvpt_koop_matrices_ctl": ([P, I64, I64, I64] + [P] * 15, ctypes.c_int),
+    "nvpt_koop_matrices_ctl": ([P, I64, I64, I64] + [P] * 14, ctypes.c_int),
     "nvpt_bamat": ([P] + [P] * 7 + [I64, I64, P, P, I64, I64, I64], ctypes.c_int),
     "nvpt_bbmat": ([P] + [P] * 6 + [I64, I64, P, P, I64], ctypes.c_int),
     "nvpt_bcmat": ([P] + [P] * 6 + [I64, I64, P, P, I64], ctypes.c_int),
@@ -59,7 +68,7 @@ _SIGS = {
     "nvpt_bro2_d": ([P, P, P, I64, I64, I64, P], ctypes.c_int),
     "nvpt_bro1_d": ([P, P, P, I64, I64, I64, P], ctypes.c_int),
     "nvpt_get_aj_atwo_d": ([P, P, I64, I64, I64, P, P, P, I64, P], ctypes.c_int),
-    "nvpt_koop_matrices_ctl_d": ([P, I64, I64, I64] + [P] * 15 + [P], ctypes.c_int),
+    "nvpt_koop_matrices_ctl_d": ([P, I64, I64, I64] + [P] * 14 + [P], ctypes.c_int),
     "nvpt_bamat_d": ([P] + [P] * 7 + [I64, I64, P, P, I64, I64, I64, P], ctypes.c_int),
     "nvpt_bbmat_d": ([P] + [P] * 6 + [I64, I64, P, P, I64, P], ctypes.c_int),
     "nvpt_bcmat_d": ([P] + [P] * 6 + [I64, I64, P, P, I64, P], ctypes.c_int),

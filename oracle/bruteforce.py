@@ -135,3 +135,14 @@ def casci(n: int, na: int, nb: int, h: np.ndarray, g: np.ndarray, nroots: int = 
     amask = np.array([a for a, _ in dets], dtype=np.uint32)
     bmask = np.array([b for _, b in dets], dtype=np.uint32)
     return amask, bmask, np.asfortranarray(V[:, :nroots]), w[:nroots]
+
+
+def expect_e_product(n: int, amask, bmask, coef, pairs) -> float:
+    """<Psi| E_{p1 q1} E_{p2 q2} ... |Psi> for 0-based orbital pairs."""
+    st = {}
+    for a, b, x in zip(amask, bmask, coef):
+        st[int(a) | (int(b) << n)] = float(x)
+    ket = dict(st)
+    for p, q in reversed(list(pairs)):
+        ket = _epq(ket, n, p, q)
+    return _dot(st, ket)
