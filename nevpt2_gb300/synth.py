@@ -213,6 +213,27 @@ def rdms(n: int, amask, bmask, coef, with_ro4: bool = True):
     return dal, taa, daaa, ro4
 
 
+def transition_rdms(n: int, amask, bmask, coef):
+    """Transition 1-3-RDMs for every root pair (big > small), stored at pair
+    index big*(big-1)/2 + small (the reference's iroot > jroot loop,
+    src/koopro4QD.F90:433) with bra = the smaller root:
+    daoff[k,i,j] = <Psi_small| E_ij |Psi_big>, and likewise for 2 and 3."""
+    lib = _rdmgen()
+    coef = np.asfortranarray(coef, dtype=np.float64)
+    nd, metat = coef.shape
+    P = metat * (metat - 1) // 2
+    amask = np.ascontiguousarray(amask, dtype=np.uint32)
+    bmask = np.ascontiguousarray(bmask, dtype=np.uint32)
+    out = [np.zeros((P,) + (n,) * (2 * k), order="F") for k in (1, 2, 3)]
+    for big in range(metat):
+        for small in range(big):
+            kpair = big * (big - 1) // 2 + small
+            for k, arr in zip((1, 2, 3), out):
+                if lib.rdmgen_dense(n, k, nd, amask, bmask, _dptr(coef), small, big, _dptr(arr), P, kpair):
+                    raise RuntimeError("rdmgen_dense failed")
+    return out
+
+
 def with_ci(p: Problem, amask, bmask, coef) -> Problem:
     """Same integrals, different CI expansion (RDMs recomputed)."""
     dal, taa, daaa, ro4 = rdms(p.nact, amask, bmask, coef, with_ro4=p.ro4 is not None)

@@ -1,0 +1,1156 @@
+"""CPU oracle of the NEVPT2 energy stage (stage 2 of the reference, QDnevpt2.x).
+
+TEST INFRASTRUCTURE ONLY: the checker of the CUDA stage-2 path and the scalar
+CPU baseline of the benchmark.  It restates src/qdnevpt.F for the
+Cholesky-integral, C1 (nsym = 1) path that the synthetic configurations use:
+
+  qdnevpt :369-698           core / virtual Fock operators and their
+                             eigendecomposition (dsyev) -> epsnew, ccore, cvirt
+  cholesky_transform :7599   half-transformed DF vectors (active untouched,
+                             virtual-virtual block never formed)
+  newint_*_cholesky :7726    integral batches as DF dot products
+  newint_ir/ia/ar :7010...   transformed one-electron integrals
+  v0 :1661                   class (0)   core^2 -> virt^2, SC == PC
+  v1k :1775, e2p1cont :3076  class (+1)
+  vm1k :2095, e2m1cont :2400 class (-1)
+  v2mod :3256, e2p2cont :2804, e2p2contp :2936     class (+2)
+  vm2mod :3685, e2m2cont :2563, e2m2contp :2688    class (-2)
+  vpupE :5437, e21pcont :5001, fillcp1p :4296      class (+1')
+  vmupE :5869, e2m1pcont :5214, fillcm1p :4266     class (-1')
+  v0pmod :4326, e20pcont :4771, fillc0p :4195      class (0')
+  caux0p :4744                                     PC metric pseudo-inverse
+  local accessors :6448-6519 (index-swapped eee2/ee2/ee2tr/ee2tl, eee2t, ro2toff)
+
+Every sum of the reference is kept (the same index pairs, the same special
+cases r = s / i = j, the same thresholds 1e-14 / 0 on the norms, the same
+zero-denominator guards); loops over the innermost indices are vectorised
+with numpy.  Symmetric eigenproblems use the upper triangle, as dsyev('V','U')
+and dsymm('L','U') do.
+
+Parity status: the reference cannot be compiled here, so this restatement is
+"parity unpinned" against the reference binary.  It is pinned by the
+reference's invariant that class (0) is identical in SC and PC
+(src/qdnevpt.F:1755-1761), by the integer metric-rank counts nnew, and by
+cross-checks between the SC and PC forms on tiny spaces.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+import scipy.linalg as sla
+
+CLASSES = ["(0)", "(+1)", "(-1)", "(+2)", "(-2)", "(+1)'", "(-1)'", "(0)'"]
+
+
+# --------------------------------------------------------------------------
+# helpers
+def tri(i, j):
+    """indice(i,j) of the reference, 0-based in and out."""
+    mx, mn = max(i, j), min(i, j)
+    return (mx + 1) * mx // 2 + mn
+
+
+def unpack_tri(v, norb):
+    h = np.zeros((norb, norb))
+    k = 0
+    for p in range(norb):
+        h[p, : p + 1] = v[k:k + p + 1]
+        h[: p + 1, p] = v[k:k + p + 1]
+        k += p + 1
+    return h
+
+
+def dense_B(chol, norb):
+    """B[Q,p,q] from cholesky_array(Q, norb(norb+1)/2)."""
+    Q = chol.shape[0]
+    B = np.zeros((Q, norb, norb))
+    k = 0
+    for p in range(norb):
+        B[:, p, : p + 1] = chol[:, k:k + p + 1]
+        B[:, : p + 1, p] = chol[:, k:k + p + 1]
+        k += p + 1
+    return B
+
+
+def upper_sym(A):
+    return np.triu(A) + np.triu(A, 1).T
+
+
+def dsyev_u(A):
+    """dsyev('V','U'): eigenpairs of the matrix whose upper triangle is A's."""
+    return sla.eigh(upper_sym(A), lower=False)
+
+
+def pc_transform(S, K, thr):
+    """The PC metric sequence shared by every class (e.g. src/qdnevpt.F:1963-2033):
+    dsyev(S); drop eigenvalues < thr (negative ones counted too, caux0p keeps
+    w >= thr); X = U w^-1/2; K~ = X^T K X (dsymm 'U' + dgemm); dsyev(K~);
+    C = X V.  Returns (C padded with zero columns to S's size, w with the
+    reference's layout: first nnew entries the K~ eigenvalues, then the
+    metric eigenvalues the second dsyev did not overwrite, nnew)."""
+    nd = S.shape[0]
+    w, V = dsyev_u(S)
+    keep = w >= thr
+    nnew = int(keep.sum())
+    caux = V[:, keep] / np.sqrt(w[keep])[None, :]
+    T = caux.T @ (upper_sym(K) @ caux)
+    w2, V2 = dsyev_u(T) if nnew else (np.zeros(0), np.zeros((0, 0)))
+    C = np.zeros((nd, nd))
+    C[:, :nnew] = caux @ V2
+    wout = w.copy()
+    wout[:nnew] = w2
+    return C, wout, nnew
+
+
+def pair_index(big, small):
+    """0-based position of the (big, small) state pair in the transition
+    arrays: src/koopro4QD.F90:433 loops iroot > jroot."""
+    return big * (big - 1) // 2 + small
+
+
+# --------------------------------------------------------------------------
+# accessor tensors (qdnevpt-local, index-swapped versions, :6448-6519)
+def ee2L(taa, dal):
+    """ee2(a,b,c,d) = taa(b,d,a,c) + [b==c] dal(d,a) -> tensor [a,b,c,d]."""
+    n = dal.shape[0]
+    T = np.transpose(taa, (2, 0, 3, 1)).copy()  # T[a,b,c,d] = taa[b,d,a,c]
+    for b in range(n):
+        T[:, b, b, :] += dal.T  # dal(d,a) -> [a,d]
+    return T
+
+
+def eee2L(daaa, taa, dal):
+    """eee2(a,b,c,d,e,f) = daaa(b,d,f,a,c,e) + [e==d] taa(b,f,a,c) + [e==b]
+    taa(f,d,a,c) + [b==c] taa(d,f,a,e) + [b==c][e==d] dal(f,a)."""
+    n = dal.shape[0]
+    T = np.transpose(daaa, (3, 0, 4, 1, 5, 2)).copy()  # [a,b,c,d,e,f] = daaa[b,d,f,a,c,e]
+    for e in range(n):
+        # e == d: taa(b,f,a,c) -> [a,b,c,f]
+        T[:, :, :, e, e, :] += np.transpose(taa, (2, 0, 3, 1))
+        # e == b: taa(f,d,a,c) -> [a,c,d,f]
+        T[:, e, :, :, e, :] += np.transpose(taa, (2, 3, 1, 0))
+        # b == c: taa(d,f,a,e) -> [a,d,e,f]
+        T[:, e, e, :, :, :] += np.transpose(taa, (2, 0, 3, 1))
+    for b in range(n):
+        for e in range(n):
+            T[:, b, b, e, e, :] += dal.T
+    return T
+
+
+def eee2tL(E3, E2):
+    """eee2t(a,b,c,d,e,f) = -eee2(a,b,d,c,e,f) + [c==d] 2 ee2(a,b,e,f)."""
+    n = E2.shape[0]
+    T = -np.transpose(E3, (0, 1, 3, 2, 4, 5)).copy()
+    for c in range(n):
+        T[:, :, c, c, :, :] += 2.0 * E2
+    return T
+
+
+def ee2trL(E2, dal):
+    """ee2tr(a,b,c,d) = -ee2(a,b,d,c) + [c==d] 2 dal(b,a)."""
+    n = dal.shape[0]
+    T = -np.transpose(E2, (0, 1, 3, 2)).copy()
+    for c in range(n):
+        T[:, :, c, c] += 2.0 * dal.T
+    return T
+
+
+def ee2tlL(E2, dal):
+    """ee2tl(a,b,c,d) = -ee2(b,a,c,d) + [a==b] 2 dal(d,c)."""
+    n = dal.shape[0]
+    T = -np.transpose(E2, (1, 0, 2, 3)).copy()
+    for a in range(n):
+        T[a, a, :, :] += 2.0 * dal.T
+    return T
+
+
+def ro2toff(taa, dal):
+    """ro2toff(ap,bp,a,b) = d2(ap,bp,a,b) - 2[ap==a] d1(bp,b) - 2[bp==b] d1(ap,a)
+    + [ap==b] d1(bp,a) + [bp==a] d1(ap,b)  (src/qdnevpt.F:6508)."""
+    n = dal.shape[0]
+    T = taa.copy()
+    for x in range(n):
+        T[x, :, x, :] -= 2.0 * dal
+        T[:, x, :, x] -= 2.0 * dal
+        T[x, :, :, x] += dal    # d1(bp,a) at [ap=x,bp,a,b=x] -> [bp,a]
+        T[:, x, x, :] += dal    # d1(ap,b) at [ap,bp=x,a=x,b] -> [ap,b]
+    return T
+
+
+# --------------------------------------------------------------------------
+@dataclass
+class Stage2Inputs:
+    """Everything the reference's stage 2 reads (nevpt.h5 + integrals).
+
+    Arrays are numpy arrays with the reference's shapes minus the state index
+    (lists over states / over state pairs)."""
+    ncore: int
+    nact: int
+    nvirt: int
+    oneint: np.ndarray
+    chol: np.ndarray
+    dal: list
+    taa: list
+    daaa: list
+    hrdm: list
+    ipko1: list
+    eako1: list
+    ipko2: list
+    eako2: list
+    gk0pa: list
+    gk0pd: list
+    gk0pf: list
+    amatIP: list
+    amatEA: list
+    bmatIP: list
+    bmatEA: list
+    cmatIP: list
+    cmatEA: list
+    dmatIP: list
+    dmatEA: list
+    daoff: list = field(default_factory=list)    # pairs: <small| E |big>
+    daaoff: list = field(default_factory=list)
+    ro3off: list = field(default_factory=list)
+    energies: np.ndarray | None = None
+    thr_lindep: float = 1e-6
+    frozen: tuple = ()
+
+    @property
+    def norb(self):
+        return self.ncore + self.nact + self.nvirt
+
+    @property
+    def metat(self):
+        return len(self.dal)
+
+
+@dataclass
+class Stage2Result:
+    e2mpp: np.ndarray   # (8, M) SC energy per class
+    psimpp: np.ndarray  # (8, M) SC norm per class
+    e2enp: np.ndarray   # (8, M) PC energy per class
+    psienep: np.ndarray
+    e2mp: np.ndarray    # (M, M) SC Heff (second-order part, before E)
+    e2en: np.ndarray    # (M, M) PC Heff
+    psimp: np.ndarray
+    psien: np.ndarray
+    nnew: dict          # PC metric ranks per class and state
+    epsnew: np.ndarray  # (norb, M)
+
+
+class _State:
+    """Per-state precomputations: orbitals, transformed integrals, accessors."""
+
+    def __init__(self, inp: Stage2Inputs, s: int, B: np.ndarray, h: np.ndarray):
+        nc, na, nv, norb = inp.ncore, inp.nact, inp.nvirt, inp.norb
+        self.nc, self.na, self.nv = nc, na, nv
+        core, act, virt = slice(0, nc), slice(nc, nc + na), slice(nc + na, norb)
+        g1 = inp.dal[s]
+        # Fock operators (Cholesky branch, src/qdnevpt.F:369-698)
+        Jc = np.einsum("xkk->x", B[:, core, core])
+        Ja = np.einsum("xab,ba->x", B[:, act, act], g1)
+
+        def fock(sl):
+            F = h[sl, sl].copy()
+            F += 2.0 * np.einsum("xpq,x->pq", B[:, sl, sl], Jc)
+            F -= np.einsum("xpk,xkq->pq", B[:, sl, core], B[:, core, sl])
+            F += np.einsum("xpq,x->pq", B[:, sl, sl], Ja)
+            F -= 0.5 * np.einsum("xpb,ba,xaq->pq", B[:, sl, act], g1, B[:, act, sl])
+            return F
+
+        eps = np.zeros(norb)
+        # dsyev('V','L'): the lower triangle is the one filled in the reference
+        if nc:
+            Fc = fock(core)
+            wc, Uc = sla.eigh(np.tril(Fc) + np.tril(Fc, -1).T, lower=True)
+            eps[core] = wc
+        else:
+            Uc = np.zeros((0, 0))
+        Fv = fock(virt)
+        wv, Uv = sla.eigh(np.tril(Fv) + np.tril(Fv, -1).T, lower=True)
+        eps[virt] = wv
+        self.eps = eps
+        U = np.zeros((norb, norb))
+        U[core, core] = Uc
+        U[act, act] = np.eye(na)
+        U[virt, virt] = Uv
+        # transformed DF vectors (virtual-virtual block is never formed)
+        R = np.einsum("pi,xpq,qj->xij", U, B, U, optimize=True)
+        R[:, virt, virt] = 0.0
+        self.R = R
+        self.h = U.T @ h @ U
+        self.core, self.act, self.virt = core, act, virt
+
+    def eri(self, a, b, c, d):
+        """Transformed (ab|cd) for index slices/arrays, as a dense block."""
+        return np.einsum("xab,xcd->abcd", self.R[:, a, b], self.R[:, c, d], optimize=True)
+
+
+def qdnevpt(inp: Stage2Inputs, classes=range(8), pc=True) -> Stage2Result:
+    """Stage 2 for every state (src/qdnevpt.F:858-993) plus the per-class
+    bookkeeping of the energies and norms."""
+    M = inp.metat
+    nc, na, nv, norb = inp.ncore, inp.nact, inp.nvirt, inp.norb
+    B = dense_B(inp.chol, norb)
+    h = unpack_tri(inp.oneint, norb)
+    r = Stage2Result(e2mpp=np.zeros((8, M)), psimpp=np.zeros((8, M)), e2enp=np.zeros((8, M)),
+                     psienep=np.zeros((8, M)), e2mp=np.zeros((M, M)), e2en=np.zeros((M, M)), psimp=np.zeros(M),
+                     psien=np.zeros(M), nnew={}, epsnew=np.zeros((norb, M)))
+    fro = np.zeros(norb, bool)
+    for k in inp.frozen:
+        fro[k] = True
+    for s in range(M):
+        st = _State(inp, s, B, h)
+        r.epsnew[:, s] = st.eps
+        if 0 in classes:
+            _v0(inp, st, s, r, fro)
+        if 1 in classes:
+            _v1k(inp, st, s, r, fro, pc)
+        if 2 in classes:
+            _vm1k(inp, st, s, r, fro, pc)
+        if 3 in classes:
+            _v2mod(inp, st, s, r, fro, pc)
+        if 4 in classes:
+            _vm2mod(inp, st, s, r, fro, pc)
+        if 7 in classes:
+            _v0pmod(inp, st, s, r, fro, pc)
+        if 6 in classes:
+            _vmupE(inp, st, s, r, fro, pc)
+        if 5 in classes:
+            _vpupE(inp, st, s, r, fro, pc)
+    return r
+
+
+def _off(arrs, s, j):
+    """(transition array of the pair, True if jstate < istate)."""
+    if j < s:
+        return arrs[pair_index(s, j)], True
+    return arrs[pair_index(j, s)], False
+
+
+# ---------------------------------------------------------------- class (0)
+def _v0(inp, st, s, r, fro):
+    """src/qdnevpt.F:1661-1772 v0."""
+    nc, eps = st.nc, st.eps
+    core, virt = st.core, st.virt
+    # traint(r,s) for the call with (i=ij, j=ii) = (ij r | s ii)
+    K = st.eri(core, virt, virt, core)  # K[i,r,s,j] = (i r | s j)
+    ev = eps[virt]
+    nvv = ev.size
+    ru, su = np.triu_indices(nvv)
+    for ii in range(nc):
+        if fro[ii]:
+            continue
+        for ij in range(ii, nc):
+            if fro[ij]:
+                continue
+            ab1 = K[ij, ru, su, ii]
+            ab2 = K[ij, su, ru, ii]
+            zrs = ru == su
+            zij = ii == ij
+            if zij:
+                dint = np.where(zrs, ab1, np.sqrt(2.0) * ab1)
+            else:
+                dint = np.where(zrs, np.sqrt(2.0) * ab1, 2.0 * np.sqrt(ab1**2 + ab2**2 - ab1 * ab2))
+            co = -dint / (ev[ru] + ev[su] - eps[ii] - eps[ij])
+            r.e2mp[s, s] += np.sum(dint * co)
+            r.psimp[s] += np.sum(co * co)
+            r.e2mpp[0, s] += np.sum(dint * co)
+            r.psimpp[0, s] += np.sum(co * co)
+    r.e2en[s, s] = r.e2mp[s, s]
+    r.psien[s] = r.psimp[s]
+    r.e2enp[0, s] = r.e2mpp[0, s]
+    r.psienep[0, s] = r.psimpp[0, s]
+
+
+def _accum_pc(inp, r, cls, s, e2, psi2):
+    M = inp.metat
+    r.e2enp[cls, s] += e2[s, s]
+    r.psienep[cls, s] += psi2
+    r.psien[s] += r.psienep[cls, s]
+    r.e2en[s, s] += e2[s, s]
+    for j in range(M):
+        if j != s:
+            r.e2en[j, s] += e2[j, s]
+
+
+# ---------------------------------------------------------------- class (+1)
+def _v1k(inp, st, s, r, fro, pc):
+    """src/qdnevpt.F:1775-2090 v1k (SC) and e2p1cont :3076 (PC)."""
+    M, nc, na = inp.metat, st.nc, st.na
+    eps = st.eps
+    g1 = inp.dal[s]
+    gk = inp.eako1[s]
+    core, act, virt = st.core, st.act, st.virt
+    T = st.eri(act, core, virt, core)  # T[a,i,r,j] = (a i | r j)
+    ro = 2.0 * np.eye(na) - g1  # ro(a,ap) = 2 delta - da(a,ap)
+    rooff = {}
+    for j in range(M):
+        if j != s:
+            d, lt = _off(inp.daoff, s, j)
+            rooff[j] = -(d.T if lt else d)  # j<i: -daoff(iap,ia); else -daoff(ia,iap) -> [a,ap]
+    ev = eps[virt]
+    for ii in range(nc):
+        if fro[ii]:
+            continue
+        for ij in range(ii, nc):
+            if fro[ij]:
+                continue
+            tj = T[:, ii, :, ij]   # traint(a, s)
+            tk = T[:, ij, :, ii]   # traintk(a, s)
+            if ij == ii:
+                cint = 0.5 * np.einsum("as,bs->abs", tj, tj)
+            else:
+                cint = (np.einsum("as,bs->abs", tj, tj) + np.einsum("as,bs->abs", tk, tk)
+                        - 0.5 * np.einsum("as,bs->abs", tj, tk) - 0.5 * np.einsum("as,bs->abs", tk, tj))
+            dn = 2.0 * np.einsum("ab,abs->s", ro, cint)
+            ek = np.einsum("ab,abs->s", gk, cint)
+            nz = np.abs(dn) > 0.0
+            den = np.zeros_like(dn)
+            ek = np.where(nz, ek / np.where(nz, dn, 1.0), ek)
+            den[nz] = eps[ii] + eps[ij] - ev[nz] - ek[nz]
+            co = np.where(nz, dn / np.where(nz, den, 1.0), 0.0)
+            con = np.where(nz, co / np.where(nz, den, 1.0), 0.0)
+            r.e2mp[s, s] += co.sum()
+            r.psimp[s] += con.sum()
+            r.e2mpp[1, s] += co.sum()
+            r.psimpp[1, s] += con.sum()
+            for j, roj in rooff.items():
+                dnj = 2.0 * np.einsum("ab,abs->s", roj, cint)
+                r.e2mp[j, s] += np.sum(np.where(den != 0.0, dnj / np.where(den != 0.0, den, 1.0), 0.0))
+    if not pc:
+        return
+    S = 2.0 * np.eye(na) - g1
+    C, w, nnew = pc_transform(S, 0.5 * gk, inp.thr_lindep)
+    r.nnew[(1, s)] = nnew
+    # e2p1cont: s(a,mu,j) = sum_ap ro(ap,a) coef(ap,mu)
+    sm = {s: (2.0 * np.eye(na) - g1).T @ C}
+    for j in range(M):
+        if j != s:
+            d, lt = _off(inp.daoff, s, j)
+            roj = -(d if lt else d.T)  # j<i: -daoff(a,ap); else -daoff(ap,a) -> [a,ap]
+            sm[j] = roj @ C
+    e2 = np.zeros((M, M))
+    psi2 = 0.0
+    for i in range(nc):
+        if fro[i]:
+            continue
+        for jj in range(i, nc):
+            if fro[jj]:
+                continue
+            tj = T[:, i, :, jj]
+            tk = T[:, jj, :, i]
+            deno = w[:na][None, :] + ev[:, None] - eps[i] - eps[jj]  # [r, mu]
+            if i != jj:
+                rj = {k: (tj + tk).T @ v for k, v in sm.items()}  # [r, mu]
+                rp = {k: (tj - tk).T @ v for k, v in sm.items()}
+                contri = (0.5 * rj[s] ** 2 + 1.5 * rp[s] ** 2) / deno
+                e2[s, s] -= contri.sum()
+                psi2 += (contri / deno).sum()
+                for k in sm:
+                    if k != s:
+                        e2[k, s] -= ((0.5 * rj[k] * rj[s] + 1.5 * rp[k] * rp[s]) / deno).sum()
+            else:
+                rj = {k: tj.T @ v for k, v in sm.items()}
+                contri = rj[s] ** 2 / deno
+                e2[s, s] -= contri.sum()
+                psi2 += (contri / deno).sum()
+                for k in sm:
+                    if k != s:
+                        e2[k, s] -= (rj[k] * rj[s] / deno).sum()
+    r.e2enp[1, s] = e2[s, s]
+    r.psienep[1, s] = psi2
+    r.psien[s] += psi2
+    r.e2en[s, s] += e2[s, s]
+    for j in range(M):
+        if j != s:
+            r.e2en[j, s] += e2[j, s]
+
+
+# ---------------------------------------------------------------- class (-1)
+def _vm1k(inp, st, s, r, fro, pc):
+    """src/qdnevpt.F:2095-2396 vm1k (SC) and e2m1cont :2400 (PC)."""
+    M, nc, na, nv = inp.metat, st.nc, st.na, st.nv
+    eps = st.eps
+    g1 = inp.dal[s]
+    gk = inp.ipko1[s]
+    core, act, virt = st.core, st.act, st.virt
+    T = st.eri(virt, core, virt, act)  # T[r,i,s,a] = (r i | s a)
+    ev = eps[virt]
+    ec = eps[core]
+    rooff = {}
+    for j in range(M):
+        if j != s:
+            d, lt = _off(inp.daoff, s, j)
+            rooff[j] = d if lt else d.T  # j<i: daoff(ia,iap); else daoff(iap,ia) -> [a,ap]
+    for ir in range(nv):
+        for is_ in range(ir, nv):
+            tj = T[ir, :, is_, :]  # traint(i,a)
+            tk = T[is_, :, ir, :]  # traintk(i,a)
+            if ir == is_:
+                cint = 0.5 * np.einsum("ia,ib->iab", tj, tj)
+            else:
+                cint = (np.einsum("ia,ib->iab", tj, tj) + np.einsum("ia,ib->iab", tk, tk)
+                        - 0.5 * np.einsum("ia,ib->iab", tj, tk) - 0.5 * np.einsum("ia,ib->iab", tk, tj))
+            dn = 2.0 * np.einsum("ab,iab->i", g1, cint)
+            ek = np.einsum("ab,iab->i", gk, cint)
+            nz = (np.abs(dn) >= 1e-14) & ~fro[:nc]
+            den = np.zeros(nc)
+            ekn = -ek[nz] / dn[nz]
+            den[nz] = ekn + ec[nz] - ev[ir] - ev[is_]
+            co = np.zeros(nc)
+            co[nz] = dn[nz] / den[nz]
+            con = np.zeros(nc)
+            con[nz] = co[nz] / den[nz]
+            r.e2mp[s, s] += co.sum()
+            r.psimp[s] += con.sum()
+            r.e2mpp[2, s] += co.sum()
+            r.psimpp[2, s] += con.sum()
+            for j, roj in rooff.items():
+                dnj = 2.0 * np.einsum("ab,iab->i", roj, cint)
+                ok = (den != 0.0) & ~fro[:nc]
+                r.e2mp[j, s] += np.sum(dnj[ok] / den[ok])
+    if not pc:
+        return
+    C, w, nnew = pc_transform(g1.copy(), 0.5 * gk, inp.thr_lindep)
+    r.nnew[(2, s)] = nnew
+    sm = {s: g1.T @ C}  # s(a,mu) = sum_ap da(ap,a) coef(ap,mu)
+    for j in range(M):
+        if j != s:
+            d, lt = _off(inp.daoff, s, j)
+            roj = d.T if lt else d  # j<i: daoff(ap,a); else daoff(a,ap) -> [a,ap]
+            sm[j] = roj @ C
+    e2 = np.zeros((M, M))
+    psi2 = 0.0
+    for ir in range(nv):
+        for is_ in range(ir, nv):
+            tj = T[ir, :, is_, :]
+            tk = T[is_, :, ir, :]
+            deno = w[:na][None, :] + ev[ir] + ev[is_] - ec[:, None]  # [i, mu]
+            live = ~fro[:nc]
+            if ir != is_:
+                rj = {k: (tj + tk) @ v for k, v in sm.items()}
+                rp = {k: (tj - tk) @ v for k, v in sm.items()}
+                contri = (0.5 * rj[s] ** 2 + 1.5 * rp[s] ** 2) / deno
+                e2[s, s] -= contri[live].sum()
+                psi2 += (contri / deno)[live].sum()
+                for k in sm:
+                    if k != s:
+                        e2[k, s] -= ((0.5 * rj[k] * rj[s] + 1.5 * rp[k] * rp[s]) / deno)[live].sum()
+            else:
+                rj = {k: tj @ v for k, v in sm.items()}
+                contri = rj[s] ** 2 / deno
+                e2[s, s] -= contri[live].sum()
+                psi2 += (contri / deno)[live].sum()
+                for k in sm:
+                    if k != s:
+                        e2[k, s] -= (rj[k] * rj[s] / deno)[live].sum()
+    r.e2enp[2, s] = e2[s, s]
+    r.psienep[2, s] = psi2
+    r.psien[s] += psi2
+    r.e2en[s, s] += e2[s, s]
+    for j in range(M):
+        if j != s:
+            r.e2en[j, s] += e2[j, s]
+
+
+# ---------------------------------------------------------------- class (+2)
+def _v2mod(inp, st, s, r, fro, pc):
+    """src/qdnevpt.F:3256-3680 v2mod (SC), e2p2cont :2804 and e2p2contp :2936 (PC)."""
+    M, nc, na = inp.metat, st.nc, st.na
+    eps = st.eps
+    daat = inp.hrdm[s]
+    gk = inp.eako2[s]
+    core, act = st.core, st.act
+    T = st.eri(core, act, core, act)  # T[i,a,j,b] = (i a | j b)
+    offs = {}
+    for j in range(M):
+        if j != s:
+            d, lt = _off(inp.daaoff, s, j)
+            d1, _ = _off(inp.daoff, s, j)
+            offs[j] = (ro2toff(d, d1), lt)
+    for ir in range(nc):
+        if fro[ir]:
+            continue
+        for is_ in range(ir, nc):
+            if fro[is_]:
+                continue
+            tr = T[ir, :, is_, :]  # traint(a,b) = (ir a | is b)
+            cint = np.einsum("pq,cd->pqcd", tr, tr)  # [cp,dp,c,d] = dint1(cp,dp)*dint2(c,d)
+            dum = daat.copy()                        # daat(cp,dp,c,d)
+            dumk = gk.copy()                         # gkp2aa(cp,dp,c,d)
+            if ir == is_:
+                cint = 0.25 * cint
+                dum = dum + np.transpose(daat, (0, 1, 3, 2))
+                dumk = dumk + np.transpose(gk, (1, 0, 2, 3))
+            dn = np.sum(cint * dum)
+            dk = np.sum(cint * dumk)
+            den = 0.0
+            if abs(dn) >= 1e-14:
+                den = eps[ir] + eps[is_] - dk / dn
+                co = dn / den
+                r.e2mp[s, s] += co
+                r.psimp[s] += co / den
+                r.e2mpp[3, s] += co
+                r.psimpp[3, s] += co / den
+            for j, (rt, lt) in offs.items():
+                if lt:   # ro2toff(cp,dp,c,d) (+ ro2toff(dp,cp,c,d))
+                    dj = rt.copy()
+                    if ir == is_:
+                        dj = dj + np.transpose(rt, (1, 0, 2, 3))
+                else:    # ro2toff(c,d,cp,dp) (+ ro2toff(c,d,dp,cp)) -> [cp,dp,c,d]
+                    dj = np.transpose(rt, (2, 3, 0, 1)).copy()
+                    if ir == is_:
+                        dj = dj + np.transpose(rt, (3, 2, 0, 1))
+                if den != 0.0:
+                    r.e2mp[j, s] += np.sum(cint * dj) / den
+    if not pc:
+        return
+    n2 = na * na
+    # (a) r != s: fillcm2 (row index (i,j) with j fastest)
+    S = daat.reshape(n2, n2)
+    Kc = gk.reshape(n2, n2)
+    C, w, nnew = pc_transform(S, Kc, inp.thr_lindep)
+    r.nnew[(3, s, "a")] = nnew
+    offt = {}
+    for j in range(M):
+        if j != s:
+            d, lt = _off(inp.daaoff, s, j)
+            d1, _ = _off(inp.daoff, s, j)
+            offt[j] = (ro2toff(d, d1), lt)
+    # s(ab,mu) = sum_{ap,bp} daat(ap,bp,a,b) coef(abp,mu)
+    sm = {s: np.einsum("pqab,pqm->abm", daat, C.reshape(na, na, n2)).reshape(n2, n2)}
+    for j, (rt, lt) in offt.items():
+        # lt: daatoff(b,a,bp,ap); else daatoff(bp,ap,b,a); as ro[a,b,ap,bp]
+        ro = np.transpose(rt, (1, 0, 3, 2)) if lt else np.transpose(rt, (3, 2, 1, 0))
+        sm[j] = np.einsum("abpq,pqm->abm", ro, C.reshape(na, na, n2)).reshape(n2, n2)
+    e2 = np.zeros((M, M))
+    psi2 = 0.0
+    for i in range(nc):
+        if fro[i]:
+            continue
+        for jj in range(i + 1, nc):
+            if fro[jj]:
+                continue
+            dint = T[i, :, jj, :].T.reshape(n2)  # dint(ab) = traint(b,a) = (i b | j a)
+            a = {k: dint @ v for k, v in sm.items()}
+            deno = w - eps[i] - eps[jj]
+            contri = a[s] ** 2 / deno
+            e2[s, s] -= contri.sum()
+            psi2 += (contri / deno).sum()
+            for k in sm:
+                if k != s:
+                    e2[k, s] -= (a[k] * a[s] / deno).sum()
+    # (b) r == s: fillcm2p on pairs a <= b
+    iu, ju = np.triu_indices(na)
+    Sfull = daat + np.transpose(daat, (0, 1, 3, 2))
+    Sp = Sfull[iu, ju][:, iu, ju]
+    Kfull = gk + np.transpose(gk, (0, 1, 3, 2))
+    Kp = Kfull[iu, ju][:, iu, ju]
+    C2, w2, nnew2 = pc_transform(Sp, Kp, inp.thr_lindep)
+    r.nnew[(3, s, "b")] = nnew2
+    # s(ab,mu) = sum_{ap<=bp} 0.5 (daat(ap,bp,a,b) + daat(ap,bp,b,a)) coef(abp,mu)
+    half = 0.5 * Sfull  # [ap,bp,a,b]
+    smp = {s: np.einsum("pq,pm->qm", half[iu, ju][:, iu, ju], C2)}
+    for j, (rt, lt) in offt.items():
+        if lt:   # 0.5 (daatoff(b,a,bp,ap) + daatoff(b,a,ap,bp)) -> [ab, abp]
+            ro = 0.5 * (np.transpose(rt, (1, 0, 3, 2)) + np.transpose(rt, (1, 0, 2, 3)))
+        else:    # 0.5 (daatoff(bp,ap,b,a) + daatoff(ap,bp,b,a))
+            ro = 0.5 * (np.transpose(rt, (3, 2, 1, 0)) + np.transpose(rt, (3, 2, 0, 1)))
+        smp[j] = ro[iu, ju][:, iu, ju] @ C2
+    for i in range(nc):
+        if fro[i]:
+            continue
+        tr = T[i, :, i, :]
+        dint = np.where(iu == ju, tr[ju, iu], 2.0 * tr[ju, iu])  # traint(b,a), doubled off-diagonal
+        a = {k: dint @ v for k, v in smp.items()}
+        deno = w2 - 2.0 * eps[i]
+        contri = a[s] ** 2 / deno
+        e2[s, s] -= contri.sum()
+        psi2 += (contri / deno).sum()
+        for k in smp:
+            if k != s:
+                e2[k, s] -= (a[k] * a[s] / deno).sum()
+    _accum_pc(inp, r, 3, s, e2, psi2)
+
+
+# ---------------------------------------------------------------- class (-2)
+def _vm2mod(inp, st, s, r, fro, pc):
+    """src/qdnevpt.F:3685-4152 vm2mod (SC), e2m2cont :2563 and e2m2contp :2688 (PC)."""
+    M, nv, na = inp.metat, st.nv, st.na
+    eps = st.eps
+    daa = inp.taa[s]
+    gk = inp.ipko2[s]
+    act, virt = st.act, st.virt
+    T = st.eri(virt, act, virt, act)  # T[r,a,s,b] = (r a | s b)
+    ev = eps[virt]
+    offs = {}
+    for j in range(M):
+        if j != s:
+            offs[j] = _off(inp.daaoff, s, j)
+    for ir in range(nv):
+        for is_ in range(ir, nv):
+            d1 = T[is_, :, ir, :]  # newint_rasb(is, ir): (is a | ir b)
+            cint = np.einsum("cd,pq->pqcd", d1, d1)
+            dum = daa.copy()
+            dumk = gk.copy()
+            if ir == is_:
+                cint = 0.25 * cint
+                dum = dum + np.transpose(daa, (0, 1, 3, 2))
+                dumk = dumk + np.transpose(gk, (1, 0, 2, 3))
+            dn = np.sum(cint * dum)
+            dk = np.sum(cint * dumk)
+            den = 0.0
+            if abs(dn) >= 1e-14:
+                den = -dk / dn - ev[ir] - ev[is_]
+                co = dn / den
+                r.e2mp[s, s] += co
+                r.psimp[s] += co / den
+                r.e2mpp[4, s] += co
+                r.psimpp[4, s] += co / den
+            for j, (d, lt) in offs.items():
+                if lt:   # daaoff(c,d,cp,dp) (+ daaoff(c,d,dp,cp)) -> [cp,dp,c,d]
+                    dj = np.transpose(d, (2, 3, 0, 1)).copy()
+                    if ir == is_:
+                        dj = dj + np.transpose(d, (3, 2, 0, 1))
+                else:    # daaoff(cp,dp,c,d) (+ daaoff(dp,cp,c,d))
+                    dj = d.copy()
+                    if ir == is_:
+                        dj = dj + np.transpose(d, (1, 0, 2, 3))
+                if den != 0.0:
+                    r.e2mp[j, s] += np.sum(cint * dj) / den
+    if not pc:
+        return
+    n2 = na * na
+    C, w, nnew = pc_transform(daa.reshape(n2, n2), gk.reshape(n2, n2), inp.thr_lindep)
+    r.nnew[(4, s, "a")] = nnew
+    sm = {s: np.einsum("pqab,pqm->abm", daa, C.reshape(na, na, n2)).reshape(n2, n2)}
+    for j, (d, lt) in offs.items():
+        # lt: daaoff(bp,ap,b,a); else daaoff(b,a,bp,ap); as ro[a,b,ap,bp]
+        ro = np.transpose(d, (3, 2, 1, 0)) if lt else np.transpose(d, (1, 0, 3, 2))
+        sm[j] = np.einsum("abpq,pqm->abm", ro, C.reshape(na, na, n2)).reshape(n2, n2)
+    e2 = np.zeros((M, M))
+    psi2 = 0.0
+    for ir in range(nv):
+        for is_ in range(ir + 1, nv):
+            d1 = T[ir, :, is_, :]  # newint_rasb(ir, is): (ir a | is b)
+            dint = d1.T.reshape(n2)  # dint1(b,a)
+            a = {k: dint @ v for k, v in sm.items()}
+            deno = w + ev[ir] + ev[is_]
+            contri = a[s] ** 2 / deno
+            e2[s, s] -= contri.sum()
+            psi2 += (contri / deno).sum()
+            for k in sm:
+                if k != s:
+                    e2[k, s] -= (a[k] * a[s] / deno).sum()
+    iu, ju = np.triu_indices(na)
+    Sfull = daa + np.transpose(daa, (0, 1, 3, 2))
+    Kfull = gk + np.transpose(gk, (0, 1, 3, 2))
+    C2, w2, nnew2 = pc_transform(Sfull[iu, ju][:, iu, ju], Kfull[iu, ju][:, iu, ju], inp.thr_lindep)
+    r.nnew[(4, s, "b")] = nnew2
+    smp = {s: (0.5 * Sfull)[iu, ju][:, iu, ju].T @ C2}
+    for j, (d, lt) in offs.items():
+        if lt:   # 0.5 (daaoff(bp,ap,b,a) + daaoff(ap,bp,b,a)) -> [ab, abp]
+            ro = 0.5 * (np.transpose(d, (3, 2, 1, 0)) + np.transpose(d, (3, 2, 0, 1)))
+        else:    # 0.5 (daaoff(b,a,ap,bp) + daaoff(b,a,bp,ap))
+            ro = 0.5 * (np.transpose(d, (1, 0, 2, 3)) + np.transpose(d, (1, 0, 3, 2)))
+        smp[j] = ro[iu, ju][:, iu, ju] @ C2
+    for ir in range(nv):
+        d1 = T[ir, :, ir, :]
+        dint = np.where(iu == ju, d1[iu, ju], 2.0 * d1[iu, ju])
+        a = {k: dint @ v for k, v in smp.items()}
+        deno = w2 + 2.0 * ev[ir]
+        contri = a[s] ** 2 / deno
+        e2[s, s] -= contri.sum()
+        psi2 += (contri / deno).sum()
+        for k in smp:
+            if k != s:
+                e2[k, s] -= (a[k] * a[s] / deno).sum()
+    _accum_pc(inp, r, 4, s, e2, psi2)
+
+
+# ---------------------------------------------------------------- class (0')
+def _v0pmod(inp, st, s, r, fro, pc):
+    """src/qdnevpt.F:4326-4740 v0pmod (SC), fillc0p :4195, e20pcont :4771 (PC)."""
+    M, nc, na, nv = inp.metat, st.nc, st.na, st.nv
+    eps = st.eps
+    g1, g2 = inp.dal[s], inp.taa[s]
+    ga, gd, gf = inp.gk0pa[s], inp.gk0pd[s], inp.gk0pf[s]
+    core, act, virt = st.core, st.act, st.virt
+    # heffd(i,r) = h'(i,r) + sum_j [2 (jj|ir) - (ji|jr)]
+    Jc = st.eri(core, core, core, virt)  # (j k | i r)
+    hd = st.h[core, virt] + 2.0 * np.einsum("jjir->ir", Jc) - np.einsum("jijr->ir", Jc)
+    DJ = st.eri(core, virt, act, act)  # (i r | a b) = djm
+    DK = st.eri(core, act, virt, act)  # (i a | r b) -> dkm(a,b) = [i,a,r,b]
+    E2 = ee2L(g2, g1)
+    E2tr = ee2trL(E2, g1)
+    # dum1[ap,bp,a,b] = ee2(bp,ap,a,b); dum2 = ee2tr(bp,b,ap,a) + [a==b] da(bp,ap)
+    dum1 = np.transpose(E2, (1, 0, 2, 3))
+    dum2 = np.transpose(E2tr, (2, 0, 3, 1)).copy()  # [ap,bp,a,b] = E2tr[bp,b,ap,a]
+    for a in range(na):
+        dum2[:, :, a, a] += g1.T  # da(bp,ap) -> [ap,bp]
+    dk1 = np.transpose(ga, (1, 0, 2, 3))  # gk0pa(bp,ap,a,b) -> [ap,bp,a,b]
+    dk2 = np.transpose(gd, (1, 0, 2, 3))
+    offs = {}
+    for j in range(M):
+        if j != s:
+            d2, _ = _off(inp.daaoff, s, j)
+            d1, _ = _off(inp.daoff, s, j)
+            E2o = ee2L(d2, d1)
+            E2tro = ee2trL(E2o, d1)
+            o1 = np.transpose(E2o, (1, 0, 2, 3))
+            o2 = np.transpose(E2tro, (2, 0, 3, 1)).copy()
+            for a in range(na):
+                o2[:, :, a, a] += d1  # daoff(ap,bp) -> [ap,bp]
+            offs[j] = (o1, o2, d1 + d1.T)
+    for ii in range(nc):
+        if fro[ii]:
+            continue
+        for irv in range(nv):
+            dj = DJ[ii, irv]          # [a,b]
+            dk = DK[ii, :, irv, :]    # [a,b]
+            # dint1[ap,bp,a,b] = 2 djp dj - djp dk - dkp dj ; dint2 = dkp dk
+            dint1 = 2 * np.einsum("pq,ab->pqab", dj, dj) - np.einsum("pq,ab->pqab", dj, dk) - \
+                np.einsum("pq,ab->pqab", dk, dj)
+            dint2 = np.einsum("pq,ab->pqab", dk, dk)
+            dint11 = np.einsum("pq,ab->pqab", dj, dj) - 0.5 * np.einsum("pq,ab->pqab", dj, dk) - \
+                0.5 * np.einsum("pq,ab->pqab", dk, dj)
+            dn = np.sum(dint1 * dum1 + dint2 * dum2)
+            dkoo = np.sum(dint11 * dk1 + dint2 * dk2)
+            di = 2.0 * dj - dk
+            dummy = np.sum(g1.T * di)
+            dummyk = np.sum(gf * 0.5 * di)
+            hh = hd[ii, irv]
+            dn += 2.0 * hh * dummy + 2.0 * hh * hh
+            dkoo += hh * dummyk
+            den = 0.0
+            if abs(dn) > 1e-14:
+                den = eps[ii] - eps[virt][irv] - dkoo / dn
+                co = dn / den
+                r.e2mp[s, s] += co
+                r.psimp[s] += co / den
+                r.e2mpp[7, s] += co
+                r.psimpp[7, s] += co / den
+            for j, (o1, o2, dsum) in offs.items():
+                dnj = np.sum(dint1 * o1 + dint2 * o2)
+                dnj += hh * np.sum(dsum.T * di)  # (daoff(b,a) + daoff(a,b)) * dint1(a,b)
+                if den != 0.0:
+                    r.e2mp[j, s] += dnj / den
+    if not pc:
+        return
+    nn = na * na
+    # fillc0p: S and K of order 2 n^2 (blocks NW, NE, SW, SE), rows ab, cols abp
+    E2loc = E2
+    Snw = 2.0 * np.transpose(E2loc, (2, 3, 1, 0)).reshape(nn, nn)
+    Sne = -np.transpose(E2loc, (2, 3, 1, 0)).reshape(nn, nn)
+    Sse = -np.einsum("qabp->abpq", g2).copy()  # -daa(bp,a,b,ap) at [a,b,ap,bp]
+    for a in range(na):
+        Sse[a, :, a, :] += 2.0 * g1.T  # 2 da(bp,b) -> [b,bp]
+    Sse = Sse.reshape(nn, nn)
+    S = np.block([[Snw, Sne], [Sne, Sse]])
+    Kga = np.transpose(ga, (1, 0, 2, 3)).reshape(nn, nn)  # ga(b,a,ap,bp) -> [a,b,ap,bp]
+    Kgd = np.transpose(gd, (1, 0, 2, 3)).reshape(nn, nn)
+    K = np.block([[Kga, -0.5 * Kga], [-0.5 * Kga, Kgd]])
+    C, w, nnew = pc_transform(S, K, inp.thr_lindep)
+    r.nnew[(7, s)] = nnew
+    nn2 = 2 * nn
+    # e20pcont auxiliaries: s, sp, spp (nn x nn2)
+    val = np.transpose(E2, (2, 3, 1, 0)).reshape(nn, nn)  # ee2(bp,ap,a,b) at [ab, abp]
+    val2 = -np.einsum("pbaq->abpq", g2).copy()
+    for a in range(na):
+        val2[a, :, a, :] += 2.0 * g1  # 2 da(b,bp)
+    val2 = val2.reshape(nn, nn)
+    aux = {s: (val @ C[:nn], val @ C[nn:], val2 @ C[nn:])}
+    for j in range(M):
+        if j == s:
+            continue
+        d2, lt = _off(inp.daaoff, s, j)
+        d1, _ = _off(inp.daoff, s, j)
+        E2o = ee2L(d2, d1)
+        if lt:   # val = ee2(b,a,ap,bp); val2 = -daaoff(a,bp,ap,b) + [ap==a] 2 daoff(bp,b)
+            v = np.transpose(E2o, (1, 0, 2, 3)).reshape(nn, nn)
+            v2 = -np.einsum("aqpb->abpq", d2).copy()
+            for a in range(na):
+                v2[a, :, a, :] += 2.0 * d1.T
+        else:    # val = ee2(bp,ap,a,b); val2 = -daaoff(ap,b,a,bp) + [ap==a] 2 daoff(b,bp)
+            v = np.transpose(E2o, (2, 3, 1, 0)).reshape(nn, nn)
+            v2 = -np.einsum("pbaq->abpq", d2).copy()
+            for a in range(na):
+                v2[a, :, a, :] += 2.0 * d1
+        v2 = v2.reshape(nn, nn)
+        aux[j] = (v @ C[:nn], v @ C[nn:], v2 @ C[nn:])
+    rooff = {}
+    for j in range(M):
+        if j != s:
+            d1, lt = _off(inp.daoff, s, j)
+            rooff[j] = (d1.T if lt else d1).reshape(nn)  # daoff(b,a) (j<i) / daoff(a,b): at [ab]
+    e2 = np.zeros((M, M))
+    psi2 = 0.0
+    ev = eps[virt]
+    gba = g1.T.reshape(nn)  # da(b,a) at [ab]
+    for i in range(nc):
+        if fro[i]:
+            continue
+        for irv in range(nv):
+            dj = DJ[i, irv].reshape(nn)
+            dk = DK[i, :, irv, :].reshape(nn)
+            hir = hd[i, irv]
+            x = 2.0 * dj - dk
+            rim = {}
+            for k, (sk, spk, sppk) in aux.items():
+                ro = gba if k == s else rooff[k]
+                rim[k] = (x @ sk + 2.0 * hir * (ro @ C[:nn])) + \
+                    (-dj @ spk + dk @ sppk - hir * (ro @ C[nn:]))
+            deno = w + ev[irv] - eps[i]
+            co = rim[s]
+            cir = co / deno
+            e2[s, s] -= (co * cir).sum()
+            psi2 += (cir ** 2).sum()
+            for k in rim:
+                if k != s:
+                    e2[k, s] -= (rim[k] * rim[s] / deno).sum()
+    r.e2enp[7, s] = e2[s, s]
+    r.psienep[7, s] = psi2
+    r.psien[s] += psi2
+    r.e2en[s, s] += e2[s, s]
+    for j in range(M):
+        if j != s:
+            r.e2en[j, s] += e2[j, s]
+
+
+# ---------------------------------------------------------------- class (-1')
+def _vmupE(inp, st, s, r, fro, pc):
+    """src/qdnevpt.F:5869-6445 vmupE (SC), fillcm1p :4266, e2m1pcont :5214 (PC)."""
+    M, nc, na, nv = inp.metat, st.nc, st.na, st.nv
+    eps = st.eps
+    g1, g2, g3 = inp.dal[s], inp.taa[s], inp.daaa[s]
+    A, Bm, Cm, Dm = inp.amatIP[s], inp.bmatIP[s], inp.cmatIP[s], inp.dmatIP[s]
+    core, act, virt = st.core, st.act, st.virt
+    # heffd(a,r) = h'(a,r) + sum_j [2 (ar|jj) - (aj|rj)] - sum_b (ab|br)
+    X1 = st.eri(act, virt, core, core)
+    X2 = st.eri(act, core, virt, core)
+    X3 = st.eri(act, act, act, virt)
+    hd = st.h[act, virt] + 2.0 * np.einsum("arjj->ar", X1) - np.einsum("ajrj->ar", X2) - np.einsum("abbr->ar", X3)
+    E2 = ee2L(g2, g1)
+    E3 = eee2L(g3, g2, g1)
+    n = na
+    # dint1(a,b,c) = (ab|cr) = X3[a,b,c,r]
+    # dumm = h^T g1^T h + 2 sum dint1(ap,cp,bp) ee2(cp,ap,bp,a) h(a) + sum dint1(ap,cp,bp) eee2(cp,ap,bp,b,a,c) dint1(a,c,b)
+    W2 = np.transpose(E2, (1, 2, 0, 3))           # [ap,bp,cp,a] = ee2(cp,ap,bp,a)
+    W3 = np.transpose(E3, (1, 2, 0, 4, 3, 5))     # [ap,bp,cp,a,b,c] = eee2(cp,ap,bp,b,a,c)
+    Bc = Bm + np.transpose(Cm, (1, 2, 3, 0))      # bmat(ap,bp,cp,a) + cmat(a,ap,bp,cp)
+    offs = {}
+    for j in range(M):
+        if j != s:
+            d3, lt = _off(inp.ro3off, s, j)
+            d2, _ = _off(inp.daaoff, s, j)
+            d1, _ = _off(inp.daoff, s, j)
+            E2o = ee2L(d2, d1)
+            E3o = eee2L(d3, d2, d1)
+            g1o = d1.T if lt else d1  # h(ap) daoff(a,ap) h(a) for j<i, daoff(ap,a) otherwise: [ap,a]
+            # ee2(cp,ap,bp,a) + ee2(a,bp,ap,cp) at [ap,bp,cp,a]
+            W2o = np.einsum("CABD->ABCD", E2o) + np.einsum("ABCD->CBDA", E2o)
+            # j<i: eee2(cp,ap,bp,b,a,c); j>i: eee2(c,a,b,bp,ap,cp); at [ap,bp,cp,a,b,c]
+            W3o = np.transpose(E3o, (1, 2, 0, 4, 3, 5)) if lt else np.transpose(E3o, (4, 3, 5, 1, 2, 0))
+            offs[j] = (g1o, W2o, W3o)
+    for irv in range(nv):
+        d = X3[:, :, :, irv]             # dint1[a,b,c]
+        hv = hd[:, irv]
+        dp = np.transpose(d, (0, 2, 1))  # dint1(ap,cp,bp) as [ap,bp,cp]
+        dumm = np.einsum("p,pa,a->", hv, g1, hv)  # h(ap) da(ap,a) h(a)
+        dumm += 2.0 * np.einsum("pqr,pqra,a->", dp, W2, hv)
+        dumm += np.einsum("pqr,pqrabc,abc->", dp, W3, dp)
+        dumk = np.einsum("p,pa,a->", hv, Dm, hv)
+        dumk += np.einsum("pqr,pqra,a->", dp, Bc, hv)
+        dumk += np.einsum("pqr,pqrabc,abc->", dp, A, dp)
+        den = 0.0
+        if dumm != 0.0:
+            den = -dumk / dumm - eps[virt][irv]
+            co = dumm / den
+            r.e2mp[s, s] += co
+            r.psimp[s] += co / den
+            r.e2mpp[6, s] += co
+            r.psimpp[6, s] += co / den
+        for j, (g1o, W2o, W3o) in offs.items():
+            dj = np.einsum("p,pa,a->", hv, g1o, hv) + np.einsum("pqr,pqra,a->", dp, W2o, hv) + \
+                np.einsum("pqr,pqrabc,abc->", dp, W3o, dp)
+            if den != 0.0:
+                r.e2mp[j, s] += dj / den
+    if not pc:
+        return
+    n3 = n ** 3
+    # fillcm1p: coef(abc,abcp) = amat(ap,bp,cp,a,b,c); s(abc,abcp) = eee2(cp,ap,bp,b,a,c); abc = c fastest
+    S = np.transpose(W3, (3, 4, 5, 0, 1, 2)).reshape(n3, n3)
+    K = np.transpose(A, (3, 4, 5, 0, 1, 2)).reshape(n3, n3)
+    C, w, nnew = pc_transform(S, K, inp.thr_lindep)
+    r.nnew[(6, s)] = nnew
+    # e2m1pcont: s(mu,abc) = sum_abcp eee2(cp,ap,bp,b,a,c) coefT(mu,abcp) = (S @ C)[abc, mu]
+    sm = {s: (S @ C, np.transpose(W2, (3, 0, 1, 2)).reshape(n, n3) @ C)}
+    for j in range(M):
+        if j == s:
+            continue
+        d3, lt = _off(inp.ro3off, s, j)
+        d2, _ = _off(inp.daaoff, s, j)
+        d1, _ = _off(inp.daoff, s, j)
+        E2o = ee2L(d2, d1)
+        E3o = eee2L(d3, d2, d1)
+        if lt:   # eee2(c,a,b,bp,ap,cp); ee2(a,bp,ap,cp)
+            W3o = np.transpose(E3o, (4, 3, 5, 1, 2, 0))
+            W2o = np.einsum("ABCD->CBDA", E2o)
+        else:    # eee2(cp,ap,bp,b,a,c); ee2(cp,ap,bp,a)
+            W3o = np.transpose(E3o, (1, 2, 0, 4, 3, 5))
+            W2o = np.einsum("CABD->ABCD", E2o)
+        So = np.transpose(W3o, (3, 4, 5, 0, 1, 2)).reshape(n3, n3)
+        sm[j] = (So @ C, np.transpose(W2o, (3, 0, 1, 2)).reshape(n, n3) @ C)
+    e2 = np.zeros((M, M))
+    psi2 = 0.0
+    for irv in range(nv):
+        d = X3[:, :, :, irv]
+        rabc = np.transpose(d, (0, 2, 1)).reshape(n3)  # dint1(a,c,b) at abc (c fastest)
+        hv = hd[:, irv]
+        rm = {k: hv @ spk + rabc @ sk for k, (sk, spk) in sm.items()}
+        deno = w + eps[virt][irv]
+        co = rm[s] / deno
+        e2[s, s] -= (rm[s] * co).sum()
+        psi2 += (co ** 2).sum()
+        for k in rm:
+            if k != s:
+                e2[k, s] -= (rm[s] * (rm[k] / deno)).sum()
+    r.e2enp[6, s] = e2[s, s]
+    r.psienep[6, s] = psi2
+    r.psien[s] += psi2
+    r.e2en[s, s] += e2[s, s]
+    for j in range(M):
+        if j != s:
+            r.e2en[j, s] += e2[j, s]
+
+
+# ---------------------------------------------------------------- class (+1')
+def _vpupE(inp, st, s, r, fro, pc):
+    """src/qdnevpt.F:5437-5865 vpupE (SC), fillcp1p :4296, e21pcont :5001 (PC)."""
+    M, nc, na = inp.metat, st.nc, st.na
+    eps = st.eps
+    g1, g2, g3 = inp.dal[s], inp.taa[s], inp.daaa[s]
+    A, Bm, Cm, Dm = inp.amatEA[s], inp.bmatEA[s], inp.cmatEA[s], inp.dmatEA[s]
+    core, act = st.core, st.act
+    n = na
+    # heffd(i,a) = h'(i,a) + sum_j [2 (jj|ia) - (ji|ja)]
+    Y = st.eri(core, core, core, act)
+    hd = st.h[core, act] + 2.0 * np.einsum("jjia->ia", Y) - np.einsum("jija->ia", Y)
+    X = st.eri(act, act, act, core)  # dint1(a,b,c) = (a b | c i)
+    E2 = ee2L(g2, g1)
+    E3 = eee2L(g3, g2, g1)
+    E2tr = ee2trL(E2, g1)
+    E3t = eee2tL(E3, E2)
+    W2 = np.transpose(E2tr, (1, 2, 0, 3))        # ee2tr(cp,ap,bp,a) -> [ap,bp,cp,a]
+    W3 = np.transpose(E3t, (1, 2, 0, 4, 3, 5))   # eee2t(cp,ap,bp,b,a,c) -> [ap,bp,cp,a,b,c]
+    Bc = Bm + np.transpose(Cm, (1, 2, 3, 0))
+    rod = 2.0 * np.eye(n) - g1                   # rodum(ap,a) = 2 delta - da(ap,a)
+    offs = {}
+    for j in range(M):
+        if j == s:
+            continue
+        d3, lt = _off(inp.ro3off, s, j)
+        d2, _ = _off(inp.daaoff, s, j)
+        d1, _ = _off(inp.daoff, s, j)
+        E2o = ee2L(d2, d1)
+        E3o = eee2L(d3, d2, d1)
+        rodo = -(d1 if lt else d1.T)             # j<i: -daoff(ap,a); else -daoff(a,ap): [ap,a]
+        # ee2tr(cp,ap,bp,a) + ee2tl(a,bp,ap,cp) at [ap,bp,cp,a]
+        W2o = np.einsum("CABD->ABCD", ee2trL(E2o, d1)) + np.einsum("ABCD->CBDA", ee2tlL(E2o, d1))
+        E3to = eee2tL(E3o, E2o)
+        # j<i: eee2t(cp,ap,bp,b,a,c); j>i: eee2t(c,a,b,bp,ap,cp)
+        W3o = np.transpose(E3to, (1, 2, 0, 4, 3, 5)) if lt else np.transpose(E3to, (4, 3, 5, 1, 2, 0))
+        offs[j] = (rodo, W2o, W3o)
+    for ii in range(nc):
+        if fro[ii]:
+            continue
+        d = X[:, :, :, ii]
+        dp = np.transpose(d, (0, 2, 1))
+        hv = hd[ii]
+        dumm = np.einsum("p,pa,a->", hv, rod, hv)
+        dumm += 2.0 * np.einsum("pqr,pqra,a->", dp, W2, hv)
+        dumm += np.einsum("pqr,pqrabc,abc->", dp, W3, dp)
+        dumk = np.einsum("p,pa,a->", hv, Dm, hv)
+        dumk += np.einsum("pqr,pqra,a->", dp, Bc, hv)
+        dumk += np.einsum("pqr,pqrabc,abc->", dp, A, dp)
+        den = 0.0
+        if dumm != 0.0:
+            den = eps[ii] - dumk / dumm
+            co = dumm / den
+            r.e2mp[s, s] += co
+            r.psimp[s] += co / den
+            r.e2mpp[5, s] += co
+            r.psimpp[5, s] += co / den
+        for j, (rodo, W2o, W3o) in offs.items():
+            dj = np.einsum("p,pa,a->", hv, rodo, hv) + np.einsum("pqr,pqra,a->", dp, W2o, hv) + \
+                np.einsum("pqr,pqrabc,abc->", dp, W3o, dp)
+            if den != 0.0:
+                r.e2mp[j, s] += dj / den
+    if not pc:
+        return
+    n3 = n ** 3
+    S = np.transpose(W3, (3, 4, 5, 0, 1, 2)).reshape(n3, n3)
+    K = np.transpose(A, (3, 4, 5, 0, 1, 2)).reshape(n3, n3)
+    C, w, nnew = pc_transform(S, K, inp.thr_lindep)
+    r.nnew[(5, s)] = nnew
+    sm = {s: (S @ C, np.transpose(W2, (3, 0, 1, 2)).reshape(n, n3) @ C)}
+    for j in range(M):
+        if j == s:
+            continue
+        d3, lt = _off(inp.ro3off, s, j)
+        d2, _ = _off(inp.daaoff, s, j)
+        d1, _ = _off(inp.daoff, s, j)
+        E2o = ee2L(d2, d1)
+        E3to = eee2tL(eee2L(d3, d2, d1), E2o)
+        if lt:   # eee2t(c,a,b,bp,ap,cp); ee2tl(a,bp,ap,cp)
+            W3o = np.transpose(E3to, (4, 3, 5, 1, 2, 0))
+            W2o = np.einsum("ABCD->CBDA", ee2tlL(E2o, d1))
+        else:    # eee2t(cp,ap,bp,b,a,c); ee2tr(cp,ap,bp,a)
+            W3o = np.transpose(E3to, (1, 2, 0, 4, 3, 5))
+            W2o = np.transpose(ee2trL(E2o, d1), (1, 2, 0, 3))
+        So = np.transpose(W3o, (3, 4, 5, 0, 1, 2)).reshape(n3, n3)
+        sm[j] = (So @ C, np.transpose(W2o, (3, 0, 1, 2)).reshape(n, n3) @ C)
+    e2 = np.zeros((M, M))
+    psi2 = 0.0
+    for ii in range(nc):
+        if fro[ii]:
+            continue
+        d = X[:, :, :, ii]
+        rabc = np.transpose(d, (0, 2, 1)).reshape(n3)
+        hv = hd[ii]
+        am = {k: hv @ spk + rabc @ sk for k, (sk, spk) in sm.items()}
+        deno = w - eps[ii]
+        co = am[s] / deno
+        e2[s, s] -= (am[s] * co).sum()
+        psi2 += (co ** 2).sum()
+        for k in am:
+            if k != s:
+                e2[k, s] -= (am[s] * (am[k] / deno)).sum()
+    r.e2enp[5, s] = e2[s, s]
+    r.psienep[5, s] = psi2
+    r.psien[s] += psi2
+    r.e2en[s, s] += e2[s, s]
+    for j in range(M):
+        if j != s:
+            r.e2en[j, s] += e2[j, s]
+
+
+# --------------------------------------------------------------------------
+def inputs_from(problem, koop: dict, thr_lindep: float = 1e-6, transition=None) -> Stage2Inputs:
+    """Stage2Inputs from a synthetic problem and the stage-1 datasets
+    (keys as the nevpt.h5 dataset names, arrays with the state index first)."""
+    p = problem
+    M = p.metat
+    g = lambda k: [np.asarray(koop[k])[s] for s in range(M)]
+    inp = Stage2Inputs(ncore=p.ncore, nact=p.nact, nvirt=p.nvirt, oneint=p.oneint, chol=p.chol,
+                       dal=[p.dal[s] for s in range(M)], taa=[p.taa[s] for s in range(M)],
+                       daaa=[p.daaa[s] for s in range(M)], hrdm=g("2-HRDM"), ipko1=g("1-IPKO"), eako1=g("1-EAKO"),
+                       ipko2=g("2-IPKO"), eako2=g("2-EAKO"), gk0pa=g("gk0pa"), gk0pd=g("gk0pd"),
+                       gk0pf=g("gk0pf"), amatIP=g("amatIP"), amatEA=g("amatEA"), bmatIP=g("bmatIP"),
+                       bmatEA=g("bmatEA"), cmatIP=g("cmatIP"), cmatEA=g("cmatEA"), dmatIP=g("dmatIP"),
+                       dmatEA=g("dmatEA"), energies=np.asarray(p.energies), thr_lindep=thr_lindep)
+    if transition is not None:
+        inp.daoff, inp.daaoff, inp.ro3off = transition
+    return inp
