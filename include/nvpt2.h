@@ -137,6 +137,57 @@ int nvpt_bdmat_d(nvpt_context *ctx, const double *atwo, double *dmat, double *dt
                  const double *dal, int64_t nact, int64_t ncore, double *f, const double *aj, int64_t metat,
                  void *stream);
 
+
+/* ------------------------------------------------------------------ */
+/* Stage 2 (QDnevpt2.x): SC/PC-NEVPT2 energies of every state.          */
+/* ------------------------------------------------------------------ */
+
+/* Inputs of src/qdnevpt.F:15 qdnevpt for the Cholesky integral path with C1
+ * symmetry: the integrals (what readint leaves in module state) and the
+ * nevpt.h5 datasets stage 1 wrote, in their reference shapes and Fortran
+ * layouts (state index first).  class_mask selects perturber classes
+ * (bit 0 (0), 1 (+1), 2 (-1), 3 (+2), 4 (-2), 5 (+1)', 6 (-1)', 7 (0)');
+ * 0xFF runs all of them, the reference's order.  frozen (optional, NULL =
+ * none) marks frozen core orbitals (.FROZEN, zgel) with a nonzero byte per
+ * orbital.  trdm1..3 ("1-TRDM".."3-TRDM", (P,n^k), P = metat(metat-1)/2)
+ * are required when metat > 1. */
+typedef struct {
+    int64_t ncore, nact, nvirt, metat, nchovec;
+    double thr_lindep;                 /* .LINDEP (default 1e-6)         */
+    int64_t no_pc;                     /* .NO PC                          */
+    int64_t class_mask;
+    const unsigned char *frozen;
+    const double *oneint;              /* norb(norb+1)/2                  */
+    const double *cholesky_array;      /* (nchovec, norb(norb+1)/2)       */
+    const double *rdm1, *rdm2, *rdm3, *hrdm2;
+    const double *ipko1, *eako1, *ipko2, *eako2;
+    const double *gk0pa, *gk0pd, *gk0pf;
+    const double *amat_ip, *amat_ea, *bmat_ip, *bmat_ea, *cmat_ip, *cmat_ea, *dmat_ip, *dmat_ea;
+    const double *trdm1, *trdm2, *trdm3;
+} nvpt_qdnevpt_in;
+
+/* Outputs, host arrays the caller owns (any may be NULL): the COMMON
+ * /PERTURBER/ per-class energies and norms e2mpp/psimpp (SC) and
+ * e2enp/psienep (PC), (8, metat) column-major; the second-order effective
+ * Hamiltonians e2mp (SC) and e2en (PC), (metat, metat), before the reference
+ * energies are added to the diagonal (src/qdnevpt.F:1050); the norms
+ * psimp/psien (metat); epsnew (norb, metat), the canonical core and virtual
+ * orbital energies; nnew (10, metat), the PC metric ranks of classes
+ * (+1), (-1), (+2)a, (+2)b, (-2)a, (-2)b, (+1)', (-1)', (0)' (-1 if not run). */
+typedef struct {
+    double *e2mpp, *psimpp, *e2enp, *psienep;
+    double *e2mp, *e2en, *psimp, *psien, *epsnew;
+    int64_t *nnew;
+} nvpt_qdnevpt_out;
+
+/* src/qdnevpt.F:858-993, the per-state loop of qdnevpt (integral transforms,
+ * core/virtual Fock eigensolves and the eight classes), for every state.
+ * The QD effective-Hamiltonian diagonalisation (:1010-1230, metat x metat)
+ * stays with the caller. */
+int nvpt_qdnevpt(nvpt_context *ctx, const nvpt_qdnevpt_in *in, nvpt_qdnevpt_out *out);
+/* Same with device pointers in `in` (outputs still on the host). */
+int nvpt_qdnevpt_d(nvpt_context *ctx, const nvpt_qdnevpt_in *in, nvpt_qdnevpt_out *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -19,8 +19,8 @@ CSRC = PKG / "csrc"
 INCLUDE = PKG.parent / "include"
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
-CUDA_SOURCES = ["capi.cu", "koop_kernels.cu", "bamat.cu"]
-CUDA_HEADERS = ["eexx.cuh", "nvpt2_internal.h"]
+CUDA_SOURCES = ["capi.cu", "koop_kernels.cu", "bamat.cu", "s2_tensor.cu", "qdnevpt.cu"]
+CUDA_HEADERS = ["eexx.cuh", "nvpt2_internal.h", "s2_tensor.cuh"]
 
 
 def _nvcc() -> str:
@@ -63,7 +63,7 @@ def build_cuda(force: bool = False, verbose: bool = False) -> Path:
         if verbose and txt:
             print(txt)
     tmp = out.with_suffix(".so.tmp")
-    cmd = [nvcc, GENCODE, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"]
+    cmd = [nvcc, GENCODE, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart", "-lcublas", "-lcusolver"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {r.stdout}\n{r.stderr}")

@@ -186,6 +186,14 @@ const char *nvpt_status_string(int status) {
     }
 }
 
+const char *nvpt_context_error_set(nvpt_context *ctx, const char *msg) {
+    if (!ctx) return "";
+    ctx->err = msg ? msg : "";
+    return ctx->err.c_str();
+}
+
+void *nvpt_context_stream(nvpt_context *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
 int64_t nvpt_launch_count(const nvpt_context *ctx) { return ctx ? g_launches.load() - ctx->launches_at_create : 0; }
 
 int64_t nvpt_nwords(int64_t nact) { return nact * (nact + 1) * (nact + 2) * (nact + 3) / 24; }

@@ -1,0 +1,301 @@
+// Implementation of the device tensor toolkit (see s2_tensor.cuh).
+#include "s2_tensor.cuh"
+
+namespace nvpt {
+namespace s2 {
+
+namespace {
+constexpr int TPB = 256;
+inline unsigned nblk(long long n) { return (unsigned)((n + TPB - 1) / TPB); }
+
+struct PermArgs {
+    int nd;
+    long long shape[6];
+    long long stride[6];  // input stride of each output axis
+    long long off;
+};
+
+__global__ void k_permute(const double *__restrict__ in, double *__restrict__ out, PermArgs a, long long total,
+                          double alpha, int acc) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    long long x = t, src = a.off;
+    for (int k = a.nd - 1; k >= 0; --k) {
+        long long i = x % a.shape[k];
+        x /= a.shape[k];
+        src += i * a.stride[k];
+    }
+    double v = alpha * in[src];
+    out[t] = acc ? out[t] + v : v;
+}
+
+__global__ void k_fill(double *p, long long n, double v) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) p[t] = v;
+}
+
+__global__ void k_axpby(long long n, double a, const double *x, double b, const double *y, double *o) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) o[t] = a * x[t] + b * (y ? y[t] : 0.0);
+}
+
+__global__ void k_symm_upper(const double *A, long long n, double *o) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * n) return;
+    long long r = t / n, c = t % n;
+    o[t] = r <= c ? A[r * n + c] : A[c * n + r];
+}
+
+// qdnevpt-local accessors, C-ordered tensors (index arithmetic only).
+__global__ void k_ee2L(const double *taa, const double *dal, int n, double *o) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long n2 = (long long)n * n;
+    if (t >= n2 * n2) return;
+    int d = t % n, c = (t / n) % n, b = (t / n2) % n, a = (int)(t / (n2 * n));
+    // ee2(a,b,c,d) = taa(b,d,a,c) + [b==c] dal(d,a)
+    double v = taa[((long long)(b * n + d) * n + a) * n + c];
+    if (b == c) v += dal[d * n + a];
+    o[t] = v;
+}
+
+__global__ void k_eee2L(const double *daaa, const double *taa, const double *dal, int n, double *o) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long n2 = (long long)n * n, n3 = n2 * n;
+    if (t >= n3 * n3) return;
+    long long x = t;
+    int f = x % n; x /= n;
+    int e = x % n; x /= n;
+    int d = x % n; x /= n;
+    int c = x % n; x /= n;
+    int b = x % n; x /= n;
+    int a = (int)x;
+    auto D2 = [&](int i, int j, int k, int l) { return taa[((long long)(i * n + j) * n + k) * n + l]; };
+    // eee2(a,b,c,d,e,f) = daaa(b,d,f,a,c,e) + [e==d] taa(b,f,a,c) + [e==b] taa(f,d,a,c)
+    //                     + [b==c] taa(d,f,a,e) + [b==c][e==d] dal(f,a)
+    double v = daaa[((((((long long)b * n + d) * n + f) * n + a) * n + c) * n) + e];
+    if (e == d) v += D2(b, f, a, c);
+    if (e == b) v += D2(f, d, a, c);
+    if (b == c) v += D2(d, f, a, e);
+    if (b == c && e == d) v += dal[f * n + a];
+    o[t] = v;
+}
+
+__global__ void k_eee2tL(const double *E3, const double *E2, int n, double *o) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long n2 = (long long)n * n, n3 = n2 * n;
+    if (t >= n3 * n3) return;
+    long long x = t;
+    int f = x % n; x /= n;
+    int e = x % n; x /= n;
+    int d = x % n; x /= n;
+    int c = x % n; x /= n;
+    int b = x % n; x /= n;
+    int a = (int)x;
+    // eee2t(a,b,c,d,e,f) = -eee2(a,b,d,c,e,f) + [c==d] 2 ee2(a,b,e,f)
+    double v = -E3[(((((long long)a * n + b) * n + d) * n + c) * n + e) * n + f];
+    if (c == d) v += 2.0 * E2[((long long)(a * n + b) * n + e) * n + f];
+    o[t] = v;
+}
+
+__global__ void k_ee2trL(const double *E2, const double *dal, int n, double *o) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long n2 = (long long)n * n;
+    if (t >= n2 * n2) return;
+    int d = t % n, c = (t / n) % n, b = (t / n2) % n, a = (int)(t / (n2 * n));
+    // ee2tr(a,b,c,d) = -ee2(a,b,d,c) + [c==d] 2 dal(b,a)
+    double v = -E2[((long long)(a * n + b) * n + d) * n + c];
+    if (c == d) v += 2.0 * dal[b * n + a];
+    o[t] = v;
+}
+
+__global__ void k_ee2tlL(const double *E2, const double *dal, int n, double *o) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long n2 = (long long)n * n;
+    if (t >= n2 * n2) return;
+    int d = t % n, c = (t / n) % n, b = (t / n2) % n, a = (int)(t / (n2 * n));
+    // ee2tl(a,b,c,d) = -ee2(b,a,c,d) + [a==b] 2 dal(d,c)
+    double v = -E2[((long long)(b * n + a) * n + c) * n + d];
+    if (a == b) v += 2.0 * dal[d * n + c];
+    o[t] = v;
+}
+
+__global__ void k_ro2toff(const double *d2, const double *d1, int n, double *o) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long n2 = (long long)n * n;
+    if (t >= n2 * n2) return;
+    int b = t % n, a = (t / n) % n, bp = (t / n2) % n, ap = (int)(t / (n2 * n));
+    double v = d2[t];
+    if (ap == a) v -= 2.0 * d1[bp * n + b];
+    if (bp == b) v -= 2.0 * d1[ap * n + a];
+    if (ap == b) v += d1[bp * n + a];
+    if (bp == a) v += d1[ap * n + b];
+    o[t] = v;
+}
+
+__global__ void k_add_diag_pairs(double *T4, int n, int pos1, int pos2, const double *M2, int transM, double alpha) {
+    // For a 4-index tensor T[i0,i1,i2,i3]: where i_pos1 == i_pos2, add
+    // alpha * M[other indices in order] (transposed if transM).
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long n2 = (long long)n * n;
+    if (t >= n2 * n2) return;
+    int idx[4] = {(int)(t / (n2 * n)), (int)((t / n2) % n), (int)((t / n) % n), (int)(t % n)};
+    if (idx[pos1] != idx[pos2]) return;
+    int o[2], k = 0;
+    for (int q = 0; q < 4; ++q)
+        if (q != pos1 && q != pos2) o[k++] = idx[q];
+    T4[t] += alpha * (transM ? M2[o[1] * n + o[0]] : M2[o[0] * n + o[1]]);
+}
+}  // namespace
+
+T alloc_v(Ctx &c, const std::vector<long long> &shape, bool zero) {
+    T t;
+    t.st = c.st;
+    t.nd = (int)shape.size();
+    for (int i = 0; i < t.nd; ++i) t.sh[i] = shape[i];
+    long long n = t.size();
+    ck(cudaMallocAsync((void **)&t.p, sizeof(double) * (size_t)(n > 0 ? n : 1), c.st), "cudaMallocAsync");
+    if (zero) ck(cudaMemsetAsync(t.p, 0, sizeof(double) * (size_t)(n > 0 ? n : 1), c.st), "memset");
+    return t;
+}
+
+T alloc(Ctx &c, std::initializer_list<long long> shape, bool zero) {
+    return alloc_v(c, std::vector<long long>(shape), zero);
+}
+
+void gather(Ctx &c, const double *in, long long off, const std::vector<long long> &shape,
+            const std::vector<long long> &stride, double *out, double alpha, bool accumulate) {
+    PermArgs a;
+    a.nd = (int)shape.size();
+    a.off = off;
+    long long total = 1;
+    for (int k = 0; k < a.nd; ++k) {
+        a.shape[k] = shape[k];
+        a.stride[k] = stride[k];
+        total *= shape[k];
+    }
+    if (total == 0) return;
+    k_permute<<<nblk(total), TPB, 0, c.st>>>(in, out, a, total, alpha, accumulate ? 1 : 0);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    ck(cudaGetLastError(), "permute launch");
+}
+
+void permute(Ctx &c, const double *in, const std::vector<long long> &in_shape, const std::vector<int> &axes,
+             double *out, double alpha, bool accumulate) {
+    int nd = (int)in_shape.size();
+    std::vector<long long> istr(nd);
+    long long s = 1;
+    for (int k = nd - 1; k >= 0; --k) {
+        istr[k] = s;
+        s *= in_shape[k];
+    }
+    std::vector<long long> shape(nd), stride(nd);
+    for (int k = 0; k < nd; ++k) {
+        shape[k] = in_shape[axes[k]];
+        stride[k] = istr[axes[k]];
+    }
+    gather(c, in, 0, shape, stride, out, alpha, accumulate);
+}
+
+T permuted(Ctx &c, const T &in, const std::vector<int> &axes, double alpha) {
+    std::vector<long long> ish(in.sh.begin(), in.sh.begin() + in.nd), osh(in.nd);
+    for (int k = 0; k < in.nd; ++k) osh[k] = ish[axes[k]];
+    T out = alloc_v(c, osh, false);
+    permute(c, in.p, ish, axes, out.p, alpha, false);
+    return out;
+}
+
+void gemm(Ctx &c, bool ta, bool tb, long long m, long long n, long long k, double alpha, const double *A, long long lda,
+          const double *B, long long ldb, double beta, double *C, long long ldc) {
+    if (m == 0 || n == 0) return;
+    // Row-major C = op(A) op(B)  <=>  column-major C^T = op(B)^T op(A)^T.
+    ck(cublasDgemm(c.blas, tb ? CUBLAS_OP_T : CUBLAS_OP_N, ta ? CUBLAS_OP_T : CUBLAS_OP_N, (int)n, (int)m, (int)k,
+                   &alpha, B, (int)ldb, A, (int)lda, &beta, C, (int)ldc),
+       "cublasDgemm");
+}
+
+void gemm_batched(Ctx &c, bool ta, bool tb, long long m, long long n, long long k, double alpha, const double *A,
+                  long long lda, long long sA, const double *B, long long ldb, long long sB, double beta, double *C,
+                  long long ldc, long long sC, long long batch) {
+    if (m == 0 || n == 0 || batch == 0) return;
+    ck(cublasDgemmStridedBatched(c.blas, tb ? CUBLAS_OP_T : CUBLAS_OP_N, ta ? CUBLAS_OP_T : CUBLAS_OP_N, (int)n,
+                                 (int)m, (int)k, &alpha, B, (int)ldb, sB, A, (int)lda, sA, &beta, C, (int)ldc, sC,
+                                 (int)batch),
+       "cublasDgemmStridedBatched");
+}
+
+void symmetrize_upper(Ctx &c, const double *A, long long n, double *out) {
+    k_symm_upper<<<nblk(n * n), TPB, 0, c.st>>>(A, n, out);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+
+void eigh_upper(Ctx &c, const double *A, long long n, double *w, double *V) {
+    if (n == 0) return;
+    // Symmetric copy, so that the triangle cuSOLVER reads is the reference's upper one.
+    symmetrize_upper(c, A, n, V);
+    int lwork = 0;
+    ck(cusolverDnDsyevd_bufferSize(c.sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, (int)n, V, (int)n, w,
+                                   &lwork),
+       "syevd_bufferSize");
+    double *work = nullptr;
+    int *info = nullptr;
+    ck(cudaMallocAsync((void **)&work, sizeof(double) * (size_t)lwork, c.st), "cudaMallocAsync");
+    ck(cudaMallocAsync((void **)&info, sizeof(int), c.st), "cudaMallocAsync");
+    ck(cusolverDnDsyevd(c.sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, (int)n, V, (int)n, w, work, lwork,
+                        info),
+       "syevd");
+    int hinfo = 0;
+    ck(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, c.st), "info copy");
+    ck(cudaStreamSynchronize(c.st), "syevd sync");
+    cudaFreeAsync(work, c.st);
+    cudaFreeAsync(info, c.st);
+    if (hinfo != 0) throw Error(2, "syevd failed, info=" + std::to_string(hinfo));
+    // The symmetric input makes row-/column-major identical; cuSOLVER stores
+    // eigenvector k as column k (column-major) = row k of the row-major array.
+}
+
+void build_ee2L(Ctx &c, const double *taa, const double *dal, int n, double *out) {
+    long long N = (long long)n * n * n * n;
+    k_ee2L<<<nblk(N), TPB, 0, c.st>>>(taa, dal, n, out);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+void build_eee2L(Ctx &c, const double *daaa, const double *taa, const double *dal, int n, double *out) {
+    long long N = (long long)n * n * n * n * n * n;
+    k_eee2L<<<nblk(N), TPB, 0, c.st>>>(daaa, taa, dal, n, out);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+void build_eee2tL(Ctx &c, const double *E3, const double *E2, int n, double *out) {
+    long long N = (long long)n * n * n * n * n * n;
+    k_eee2tL<<<nblk(N), TPB, 0, c.st>>>(E3, E2, n, out);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+void build_ee2trL(Ctx &c, const double *E2, const double *dal, int n, double *out) {
+    long long N = (long long)n * n * n * n;
+    k_ee2trL<<<nblk(N), TPB, 0, c.st>>>(E2, dal, n, out);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+void build_ee2tlL(Ctx &c, const double *E2, const double *dal, int n, double *out) {
+    long long N = (long long)n * n * n * n;
+    k_ee2tlL<<<nblk(N), TPB, 0, c.st>>>(E2, dal, n, out);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+void build_ro2toff(Ctx &c, const double *taa, const double *dal, int n, double *out) {
+    long long N = (long long)n * n * n * n;
+    k_ro2toff<<<nblk(N), TPB, 0, c.st>>>(taa, dal, n, out);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+void axpby(Ctx &c, long long count, double a, const double *x, double b, const double *y, double *out) {
+    k_axpby<<<nblk(count), TPB, 0, c.st>>>(count, a, x, b, y, out);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+void fill(Ctx &c, double *p, long long count, double v) {
+    k_fill<<<nblk(count), TPB, 0, c.st>>>(p, count, v);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+void add_diag_pairs(Ctx &c, double *T4, int n, int pos1, int pos2, const double *M2, bool transposeM, double alpha) {
+    long long N = (long long)n * n * n * n;
+    k_add_diag_pairs<<<nblk(N), TPB, 0, c.st>>>(T4, n, pos1, pos2, M2, transposeM ? 1 : 0, alpha);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+
+}  // namespace s2
+}  // namespace nvpt

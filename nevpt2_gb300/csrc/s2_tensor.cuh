@@ -1,0 +1,117 @@
+// Device tensor toolkit for the NEVPT2 energy stage.
+//
+// Tensors are dense, C-ordered (last index fastest) FP64 arrays with up to 6
+// axes.  The stage-2 algebra is expressed with four primitives: an axis
+// permutation (materialised), the accessor builders of the reference's
+// qdnevpt-local normal-ordered products (src/qdnevpt.F:6448-6519), dense
+// GEMMs (cuBLAS) and symmetric eigendecompositions (cuSOLVER syevd).  All
+// work is enqueued on one stream; allocations are stream-ordered.
+#pragma once
+#include <cublas_v2.h>
+#include <cuda_runtime.h>
+#include <cusolverDn.h>
+
+#include <array>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "nvpt2_internal.h"
+
+namespace nvpt {
+namespace s2 {
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+inline void ck(cudaError_t e, const char *what) {
+    if (e != cudaSuccess) throw Error(e == cudaErrorMemoryAllocation ? 3 : 2, std::string(what) + ": " + cudaGetErrorString(e));
+}
+inline void ck(cublasStatus_t e, const char *what) {
+    if (e != CUBLAS_STATUS_SUCCESS) throw Error(2, std::string(what) + ": cuBLAS status " + std::to_string((int)e));
+}
+inline void ck(cusolverStatus_t e, const char *what) {
+    if (e != CUSOLVER_STATUS_SUCCESS) throw Error(2, std::string(what) + ": cuSOLVER status " + std::to_string((int)e));
+}
+
+// Owning device tensor (stream-ordered allocation).
+struct T {
+    double *p = nullptr;
+    int nd = 0;
+    std::array<long long, 6> sh{{1, 1, 1, 1, 1, 1}};
+    cudaStream_t st = nullptr;
+    T() = default;
+    T(const T &) = delete;
+    T &operator=(const T &) = delete;
+    T(T &&o) noexcept { *this = std::move(o); }
+    T &operator=(T &&o) noexcept {
+        release();
+        p = o.p; nd = o.nd; sh = o.sh; st = o.st;
+        o.p = nullptr;
+        return *this;
+    }
+    ~T() { release(); }
+    void release() {
+        if (p) cudaFreeAsync(p, st);
+        p = nullptr;
+    }
+    long long size() const {
+        long long s = 1;
+        for (int i = 0; i < nd; ++i) s *= sh[i];
+        return s;
+    }
+    long long dim(int i) const { return sh[i]; }
+};
+
+struct Ctx {
+    cudaStream_t st;
+    cublasHandle_t blas;
+    cusolverDnHandle_t sol;
+};
+
+T alloc(Ctx &c, std::initializer_list<long long> shape, bool zero = true);
+T alloc_v(Ctx &c, const std::vector<long long> &shape, bool zero = true);
+// Non-owning 1-D view helpers are plain pointers.
+
+// out = alpha * permute(in, axes) (+ out if accumulate).  `in` has shape
+// in_shape (C order); axes as numpy.transpose.
+void permute(Ctx &c, const double *in, const std::vector<long long> &in_shape, const std::vector<int> &axes,
+             double *out, double alpha = 1.0, bool accumulate = false);
+T permuted(Ctx &c, const T &in, const std::vector<int> &axes, double alpha = 1.0);
+
+// Gather of a strided sub-block: out[i0..] = in[off + sum i_k * stride_k],
+// out C-ordered with shape `shape`.
+void gather(Ctx &c, const double *in, long long off, const std::vector<long long> &shape,
+            const std::vector<long long> &stride, double *out, double alpha = 1.0, bool accumulate = false);
+
+// Row-major GEMM: C[m,n] = alpha op(A)[m,k] op(B)[k,n] + beta C.
+void gemm(Ctx &c, bool ta, bool tb, long long m, long long n, long long k, double alpha, const double *A, long long lda,
+          const double *B, long long ldb, double beta, double *C, long long ldc);
+void gemm_batched(Ctx &c, bool ta, bool tb, long long m, long long n, long long k, double alpha, const double *A,
+                  long long lda, long long sA, const double *B, long long ldb, long long sB, double beta, double *C,
+                  long long ldc, long long sC, long long batch);
+
+// Symmetric eigendecomposition of the matrix whose upper triangle (row <=
+// col) is held in A (n x n, row-major), as dsyev('V','U') of the reference
+// sees it.  w ascending; V[k][i] = component i of eigenvector k.
+void eigh_upper(Ctx &c, const double *A, long long n, double *w, double *V);
+// Symmetric copy: out = triu(A) + triu(A,1)^T.
+void symmetrize_upper(Ctx &c, const double *A, long long n, double *out);
+
+// Accessor builders (C-ordered n-index tensors of one state or pair).
+void build_ee2L(Ctx &c, const double *taa, const double *dal, int n, double *out);
+void build_eee2L(Ctx &c, const double *daaa, const double *taa, const double *dal, int n, double *out);
+void build_eee2tL(Ctx &c, const double *E3, const double *E2, int n, double *out);
+void build_ee2trL(Ctx &c, const double *E2, const double *dal, int n, double *out);
+void build_ee2tlL(Ctx &c, const double *E2, const double *dal, int n, double *out);
+void build_ro2toff(Ctx &c, const double *taa, const double *dal, int n, double *out);
+
+// Elementwise helpers.
+void axpby(Ctx &c, long long count, double a, const double *x, double b, const double *y, double *out);
+void fill(Ctx &c, double *p, long long count, double v);
+void add_diag_pairs(Ctx &c, double *T4, int n, int pos1, int pos2, const double *M2, bool transposeM, double alpha);
+
+}  // namespace s2
+}  // namespace nvpt

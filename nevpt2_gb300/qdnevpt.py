@@ -1,0 +1,119 @@
+"""Host-side mirror of the reference's stage 2 (QDnevpt2.x): the per-state
+SC/PC-NEVPT2 loop of src/qdnevpt.F:858-993 on the GPU through
+``nvpt_qdnevpt``, plus the metat x metat effective-Hamiltonian step of
+:1010-1230 (dgeev, ascending sort, Hermitisation) on the host.
+
+Inputs use the nevpt.h5 dataset names and the reference's array shapes in
+numpy Fortran order (state index first).
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from ._native import Context, ptr
+from .koopro import context
+
+CLASSES = ["(0)", "(+1)", "(-1)", "(+2)", "(-2)", "(+1)'", "(-1)'", "(0)'"]
+P = ctypes.c_void_p
+I64 = ctypes.c_int64
+
+
+class _In(ctypes.Structure):
+    _fields_ = [("ncore", I64), ("nact", I64), ("nvirt", I64), ("metat", I64), ("nchovec", I64),
+                ("thr_lindep", ctypes.c_double), ("no_pc", I64), ("class_mask", I64), ("frozen", P),
+                ("oneint", P), ("cholesky_array", P), ("rdm1", P), ("rdm2", P), ("rdm3", P), ("hrdm2", P),
+                ("ipko1", P), ("eako1", P), ("ipko2", P), ("eako2", P), ("gk0pa", P), ("gk0pd", P), ("gk0pf", P),
+                ("amat_ip", P), ("amat_ea", P), ("bmat_ip", P), ("bmat_ea", P), ("cmat_ip", P), ("cmat_ea", P),
+                ("dmat_ip", P), ("dmat_ea", P), ("trdm1", P), ("trdm2", P), ("trdm3", P)]
+
+
+class _Out(ctypes.Structure):
+    _fields_ = [("e2mpp", P), ("psimpp", P), ("e2enp", P), ("psienep", P), ("e2mp", P), ("e2en", P),
+                ("psimp", P), ("psien", P), ("epsnew", P), ("nnew", P)]
+
+
+@dataclass
+class Stage2Energies:
+    e2mpp: np.ndarray
+    psimpp: np.ndarray
+    e2enp: np.ndarray
+    psienep: np.ndarray
+    e2mp: np.ndarray
+    e2en: np.ndarray
+    psimp: np.ndarray
+    psien: np.ndarray
+    epsnew: np.ndarray
+    nnew: np.ndarray
+
+
+_BOUND = False
+
+
+def _bind(ctx: Context):
+    global _BOUND
+    if not _BOUND:
+        for name in ("nvpt_qdnevpt",):
+            fn = getattr(ctx._lib, name)
+            fn.argtypes = [P, ctypes.POINTER(_In), ctypes.POINTER(_Out)]
+            fn.restype = ctypes.c_int
+        fn = ctx._lib.nvpt_qdnevpt_d
+        fn.argtypes = [P, ctypes.POINTER(_In), ctypes.POINTER(_Out), P]
+        fn.restype = ctypes.c_int
+        _BOUND = True
+
+
+def _f(a):
+    if a is None:
+        return None
+    a = np.asarray(a, dtype=np.float64)
+    return a if a.flags.f_contiguous else np.asfortranarray(a)
+
+
+def qdnevpt(problem, koop: dict, transition=None, thr_lindep: float = 1e-6, class_mask: int = 0xFF,
+            no_pc: bool = False, frozen=None) -> Stage2Energies:
+    """Per-state loop of src/qdnevpt.F:858-993 on the GPU.  ``koop`` holds
+    the stage-1 datasets by their nevpt.h5 names; ``transition`` the
+    (1-TRDM, 2-TRDM, 3-TRDM) arrays when metat > 1."""
+    ctx = context()
+    _bind(ctx)
+    p = problem
+    M, n = p.metat, p.nact
+    keep = []
+
+    def h(a):
+        a = _f(a)
+        keep.append(a)
+        return ptr(a)
+
+    g = lambda k: h(koop[k])
+    fr = None
+    if frozen is not None:
+        fm = np.zeros(p.norb, np.uint8)
+        fm[list(frozen)] = 1
+        keep.append(fm)
+        fr = ptr(fm)
+    inp = _In(p.ncore, n, p.nvirt, M, p.chol.shape[0], thr_lindep, int(no_pc), class_mask, fr, h(p.oneint),
+              h(p.chol), g("1-RDM"), g("2-RDM"), g("3-RDM"), g("2-HRDM"), g("1-IPKO"), g("1-EAKO"), g("2-IPKO"),
+              g("2-EAKO"), g("gk0pa"), g("gk0pd"), g("gk0pf"), g("amatIP"), g("amatEA"), g("bmatIP"), g("bmatEA"),
+              g("cmatIP"), g("cmatEA"), g("dmatIP"), g("dmatEA"),
+              *(h(t) for t in (transition if transition is not None else (None, None, None))))
+    res = Stage2Energies(*(np.zeros((8, M), order="F") for _ in range(4)), np.zeros((M, M), order="F"),
+                         np.zeros((M, M), order="F"), np.zeros(M), np.zeros(M), np.zeros((p.norb, M), order="F"),
+                         np.zeros((10, M), np.int64, order="F"))
+    out = _Out(*(ptr(getattr(res, k)) for k in ("e2mpp", "psimpp", "e2enp", "psienep", "e2mp", "e2en", "psimp",
+                                                  "psien", "epsnew", "nnew")))
+    ctx.check(ctx._lib.nvpt_qdnevpt(ctx.handle, ctypes.byref(inp), ctypes.byref(out)), "nvpt_qdnevpt")
+    return res
+
+
+def effective_hamiltonian(e2: np.ndarray, energies: np.ndarray):
+    """src/qdnevpt.F:1046-1126: Heff = e2 + diag(E); eigenvalues of the
+    non-Hermitian matrix (dgeev), sorted ascending by real part.  Returns
+    (sorted eigenvalues (real parts), right eigenvectors, Heff)."""
+    H = np.array(e2, dtype=np.float64) + np.diag(energies)
+    w, vr = np.linalg.eig(H)
+    order = np.argsort(w.real, kind="stable")
+    return w.real[order], vr[:, order].real, H
