@@ -57,8 +57,8 @@ def workload_desc(p):
                         f"{p.metat} state(s), DF integrals Q={p.nchovec}",
             "nact": p.nact, "nele": p.nele, "ncore": p.ncore, "nvirt": p.nvirt, "states": p.metat,
             "determinants": p.ndet, "precision": "fp64",
-            "scope": "stage 1 (Koopmans matrices: bro3/bro2/bro1, get_aj_atwo, koop_matrices_ctl, bamat, bbmat, "
-                     "bcmat, bdmat); stage 2 (SC/PC classes) not yet on the device",
+            "scope": "stage 1 (bro3/bro2/bro1, get_aj_atwo, koop_matrices_ctl, bamat, bbmat, bcmat, bdmat) + "
+                     "stage 2 (core/virtual Fock eigensolves, DF transforms, all 8 SC and PC perturber classes)",
             "l2": "inputs larger than L2 (packed 4-RDM) and a 512 MB L2 flush between timed steps"}
 
 
@@ -104,7 +104,7 @@ class Clocks:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def cpu_baseline(p, budget_s: float):
+def cpu_baseline(p, budget_s: float, koop: dict, stage2_seconds: float | None = None):
     """Times the CPU oracle (C restatement, OpenMP over all host threads) on a
     bounded sample: the full n^5-n^7 Koopmans builders plus `k` of the n^2
     (a,c) slabs of the n^9 A-matrix builder, extrapolated to the whole stage."""
@@ -134,12 +134,25 @@ def cpu_baseline(p, budget_s: float):
         k_slabs = extra
     else:
         k_slabs = threads
-    total = t_rest + t_slab * n * n
+    t_s1 = t_rest + t_slab * n * n
     del d3
+    t_s2 = stage2_seconds if stage2_seconds is not None else time_stage2_oracle(p, koop)
+    total = t_s1 + t_s2
     return {"value": total / M, "unit": "s/state", "cores": threads, "kind": "port",
-            "sample": f"C restatement of the reference loops (OpenMP, {threads} threads): every stage-1 builder "
-                      f"except bamat run in full ({t_rest:.2f} s); bamat timed on {k_slabs} of {n * n} (a,c) slabs "
-                      f"and scaled by n^2/slabs"}
+            "sample": f"stage 1: C restatement of the reference loops (OpenMP, {threads} threads), every builder "
+                      f"except bamat run in full ({t_rest:.2f} s), bamat timed on {k_slabs} of {n * n} (a,c) slabs "
+                      f"and scaled by n^2/slabs ({t_s1:.1f} s in all); stage 2: numpy/LAPACK restatement of "
+                      f"src/qdnevpt.F run in full ({t_s2:.1f} s)",
+            "stage1_s": t_s1, "stage2_s": t_s2}
+
+
+def time_stage2_oracle(p, koop):
+    """Wall time of the stage-2 oracle (all eight classes, SC and PC) on the
+    given stage-1 datasets."""
+    from oracle import qdnevpt_oracle as q
+    t0 = time.perf_counter()
+    q.qdnevpt(q.inputs_from(p, koop))
+    return time.perf_counter() - t0
 
 
 def run_reference(args):
@@ -148,9 +161,11 @@ def run_reference(args):
         return
     from nevpt2_gb300 import synth
     p = synth.config_problem(args.config)
+    koop = timing_datasets(p)
+    t_s2 = time_stage2_oracle(p, koop)  # measured once; every step re-times stage 1
     vals = []
     for i in range(args.warmup + args.steps):
-        cb = cpu_baseline(p, args.cpu_seconds)
+        cb = cpu_baseline(p, args.cpu_seconds / 4, koop, stage2_seconds=t_s2)
         if i >= args.warmup:
             vals.append(cb["value"])
     v = float(np.mean(vals))
@@ -162,6 +177,36 @@ def run_reference(args):
             "cpu_baseline": cb, "e2e": {"value": v, "unit": "s/state", "h2d_bytes_per_step": 0,
                                         "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def timing_datasets(p):
+    """Stage-1 datasets with the right shapes (values irrelevant: used to time
+    the CPU oracle of stage 2 when no GPU result is at hand)."""
+    rng = np.random.default_rng(0)
+    n, M = p.nact, p.metat
+    z = lambda *s: np.asfortranarray(rng.standard_normal(s) * 1e-3)
+    return {"2-HRDM": z(M, n, n, n, n), "1-IPKO": z(M, n, n), "1-EAKO": z(M, n, n), "2-IPKO": z(M, n, n, n, n),
+            "2-EAKO": z(M, n, n, n, n), "gk0pa": z(M, n, n, n, n), "gk0pd": z(M, n, n, n, n), "gk0pf": z(M, n, n),
+            "amatIP": z(M, *(n,) * 6), "amatEA": z(M, *(n,) * 6), "bmatIP": z(M, n, n, n, n),
+            "bmatEA": z(M, n, n, n, n), "cmatIP": z(M, n, n, n, n), "cmatEA": z(M, n, n, n, n),
+            "dmatIP": z(M, n, n), "dmatEA": z(M, n, n)}
+
+
+def fp64_peak(dev) -> float:
+    """Measured FP64 GEMM rate of this GPU (cuBLAS DGEMM through torch, 4096^3,
+    best of 5, CUDA events), TFLOP/s."""
+    import torch
+    a = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
+    b = torch.randn(4096, 4096, dtype=torch.float64, device=dev)
+    best = 1e30
+    for _ in range(6):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        best = min(best, e0.elapsed_time(e1))
+    return 2 * 4096 ** 3 / (best * 1e-3) / 1e12
 
 
 def run_ours(args):
@@ -184,9 +229,13 @@ def run_ours(args):
     st = Stage1(p, device=str(dev))
     stream = torch.cuda.Stream(dev)
     flush = torch.empty(512 * 2**20 // 4, dtype=torch.float32, device=dev)
+    def step():
+        st.run(stream)
+        return st.stage2(stream)
+
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
-            st.run(stream)
+            energies = step()
     torch.cuda.synchronize(dev)
     # bamat alone, for the roofline (same stream)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
@@ -204,7 +253,7 @@ def run_ours(args):
         for i in range(args.steps):
             flush.zero_()
             starts[i].record(stream)
-            st.run(stream)
+            energies = step()
             ends[i].record(stream)
     torch.cuda.synchronize(dev)
     launches = st.ctx.launches - launches0
@@ -239,37 +288,52 @@ def run_ours(args):
         pinned[name] = t.numpy().reshape(a.shape, order="F")
     from dataclasses import replace
     pp = replace(p, ro4=pinned["ro4"], oneint=pinned["oneint"], chol=pinned["chol"])
-    koopro.koopro4QD(pp)  # warm
+    from nevpt2_gb300 import qdnevpt as gq
+
+    def e2e_step():
+        res = koopro.koopro4QD(pp)
+        return res, gq.qdnevpt(pp, res)
+
+    e2e_step()  # warm
     e2e_t = []
     for _ in range(max(1, min(args.steps, 3))):
         t0 = time.perf_counter()
-        res = koopro.koopro4QD(pp)
+        res, en = e2e_step()
         e2e_t.append(time.perf_counter() - t0)
     e2e = float(np.mean(e2e_t)) / M
     W = p.nwords
     b8 = 8
+    # stage-1 host calls (ro4 is sent to bro3 and to bamat) + stage-2 datasets
     h2d = b8 * (2 * W * n**4 * M + p.oneint.size + p.chol.size + 6 * (M * n**6) + 10 * (M * n**4) + 10 * n**4)
-    d2h = b8 * sum(v.size for v in res.values())
+    h2d += b8 * (p.oneint.size + p.chol.size + M * (3 * n**6 + 12 * n**4 + 8 * n**2))
+    d2h = b8 * sum(v.size for v in res.values()) + b8 * (4 * 8 * M + 2 * M * M + 2 * M + p.norb * M + 10 * M)
 
     if rank != 0:
         dist.destroy_process_group() if ws > 1 else None
         return
     # roofline: bamat's algorithmic bytes per launch = 8*(live packed 4-RDM + Gamma3 + atwo + 2 outputs)
-    live = live_ro4_entries(n)
-    alg_bytes = 8 * M * (live + n**6 + 2 * n**6) + 8 * n**4
-    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
-    hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    achieved = alg_bytes / (bamat_ms * 1e-3) / 1e9
-    cb = cpu_baseline(p, args.cpu_seconds)
+    # bamat: FP64 contraction (slab unpack + cuBLAS DGEMMs); algorithmic flops of
+    # the reference loop 12n^9 + 16n^8 + 12n^7 per state
+    alg_flops = M * (12 * n**9 + 16 * n**8 + 12 * n**7)
+    peak64 = fp64_peak(dev)
+    achieved = alg_flops / (bamat_ms * 1e-3) / 1e12
+    koop = {k: st.result(k) for k in st.out}
+    koop.update({"1-RDM": p.dal, "2-RDM": p.taa, "3-RDM": p.daaa})
+    cb = cpu_baseline(p, args.cpu_seconds, koop)
     line = {"metric": METRIC, "value": ms / 1e3 / M, "unit": "s/state", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded CI vector, exact RDMs, random DF integrals)",
             "config": workload_desc(p), "gpu_launches": int(launches),
             "e2e": {"value": e2e, "unit": "s/state", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-            "roofline": {"kernel": "k_bamat_direct", "bound": "hbm", "achieved": achieved, "peak": hbm_peak,
-                         "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
-                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback",
-                         "kernel_ms": bamat_ms, "alg_bytes": alg_bytes},
+            "roofline": {"kernel": "bamat (k_bamat_slabs + cuBLAS DGEMM + k_bamat_rest)", "bound": "tensor",
+                         "achieved": achieved, "peak": peak64, "unit": "TFLOP/s", "frac": achieved / peak64,
+                         "traffic": None, "precision": "fp64",
+                         "peak_source": "FP64 DGEMM rate measured live in this run (cuBLAS 4096^3)",
+                         "kernel_ms": bamat_ms, "alg_flops": alg_flops},
+            "energies": {"e2_sc": float(energies.e2mp[0, 0]), "e2_pc": float(energies.e2en[0, 0]),
+                         "per_class_sc": [float(x) for x in energies.e2mpp[:, 0]],
+                         "per_class_pc": [float(x) for x in energies.e2enp[:, 0]],
+                         "nnew": [int(x) for x in energies.nnew[:, 0]]},
             "clocks": clk, "cpu_baseline": cb, "step_ms_all": times}
     print(json.dumps(line), flush=True)
     if ws > 1:

@@ -281,7 +281,17 @@ int nvpt_bamat_d(nvpt_context *ctx, double *amat, double *atmat, const double *a
     cudaStream_t st = pick(ctx, stream);
     Rdm r = make_rdm(nact, metat, dal, taa, daaa, ro4);
     launch_build_f(f, aj, atwo, (int)nact, (int)ncore, 1, st);
-    launch_bamat_direct(r, atwo, f, (int)ncore, amat, atmat, st);
+    // Tiny active spaces: one thread per element evaluates the reference's
+    // loop directly.  Otherwise the n^9 part runs as dense GEMMs over
+    // materialised four-operator slabs (bamat_gemm.cu).
+    if (nact <= 5) {
+        launch_bamat_direct(r, atwo, f, (int)ncore, amat, atmat, st);
+        return after_launch(ctx, "bamat");
+    }
+    int slabs = nact >= 15 ? 2 : 4;
+    int rc = launch_bamat_gemm(r, atwo, f, (int)ncore, amat, atmat, st, slabs);
+    if (rc == 2) return fail(ctx, NVPT_ENOMEM, "bamat: device allocation failed");
+    if (rc) return fail(ctx, NVPT_ECUDA, "bamat: cuBLAS GEMM failed");
     return after_launch(ctx, "bamat");
 }
 

@@ -32,6 +32,9 @@ void launch_bdmat(const Rdm &r, const double *atwo, const double *f, const doubl
                   double *dt, cudaStream_t st);
 void launch_bamat_direct(const Rdm &r, const double *atwo, const double *f, int ncore, double *amat, double *atmat,
                          cudaStream_t st);
+// Dense-contraction A-matrix builder (bamat_gemm.cu); 0 on success.
+int launch_bamat_gemm(const Rdm &r, const double *atwo, const double *f, int ncore, double *amat, double *atmat,
+                      cudaStream_t st, int slabs_per_batch);
 void launch_ord8(const int64_t *in8, int64_t *out8, int64_t *lindex, long long count, cudaStream_t st);
 
 }  // namespace nvpt

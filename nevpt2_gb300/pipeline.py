@@ -70,6 +70,33 @@ class Stage1:
         c.call("nvpt_bdmat_d", ptr(self.atwo), ptr(o["dmatIP"]), ptr(o["dmatEA"]), ptr(self.taa), ptr(self.dal), n,
                nc, ptr(self.f), ptr(self.aj), M, st)
 
+    def stage2(self, stream: torch.cuda.Stream | None = None, thr_lindep: float = 1e-6, class_mask: int = 0xFF):
+        """Run the NEVPT2 energy stage on the resident stage-1 outputs
+        (nvpt_qdnevpt_d; single-state problems, no transition RDMs)."""
+        import ctypes
+
+        from . import qdnevpt as gq
+        p, o = self.p, self.out
+        if p.metat != 1:
+            raise NotImplementedError("resident stage 2 runs single-state problems; use qdnevpt.qdnevpt for QD")
+        gq._bind(self.ctx)
+        st = ptr_stream(stream or torch.cuda.current_stream(self.device))
+        inp = gq._In(p.ncore, p.nact, p.nvirt, p.metat, p.chol.shape[0], thr_lindep, 0, class_mask, None,
+                     ptr(self.oneint), ptr(self.chol), ptr(self.dal), ptr(self.taa), ptr(self.daaa), ptr(o["2-HRDM"]),
+                     ptr(o["1-IPKO"]), ptr(o["1-EAKO"]), ptr(o["2-IPKO"]), ptr(o["2-EAKO"]), ptr(o["gk0pa"]),
+                     ptr(o["gk0pd"]), ptr(o["gk0pf"]), ptr(o["amatIP"]), ptr(o["amatEA"]), ptr(o["bmatIP"]),
+                     ptr(o["bmatEA"]), ptr(o["cmatIP"]), ptr(o["cmatEA"]), ptr(o["dmatIP"]), ptr(o["dmatEA"]),
+                     None, None, None)
+        M = p.metat
+        res = gq.Stage2Energies(*(np.zeros((8, M), order="F") for _ in range(4)), np.zeros((M, M), order="F"),
+                                np.zeros((M, M), order="F"), np.zeros(M), np.zeros(M),
+                                np.zeros((p.norb, M), order="F"), np.zeros((10, M), np.int64, order="F"))
+        out = gq._Out(*(ptr(getattr(res, k)) for k in ("e2mpp", "psimpp", "e2enp", "psienep", "e2mp", "e2en",
+                                                         "psimp", "psien", "epsnew", "nnew")))
+        self.ctx.check(self.ctx._lib.nvpt_qdnevpt_d(self.ctx.handle, ctypes.byref(inp), ctypes.byref(out), st),
+                       "nvpt_qdnevpt_d")
+        return res
+
     def result(self, name: str) -> np.ndarray:
         n, M = self.p.nact, self.p.metat
         t = self.out[name].cpu().numpy()
