@@ -43,6 +43,8 @@ def _args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default=WORKLOAD)
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the bounded CPU baseline sample")
+    ap.add_argument("--profile", action="store_true",
+                    help="run only --warmup + --steps device-resident steps, untimed (for ncu launch lists)")
     return ap.parse_args()
 
 
@@ -237,6 +239,14 @@ def run_ours(args):
         for _ in range(args.warmup):
             energies = step()
     torch.cuda.synchronize(dev)
+    if args.profile:
+        with torch.cuda.stream(stream):
+            for _ in range(args.steps):
+                energies = step()
+        torch.cuda.synchronize(dev)
+        print(json.dumps({"profile": args.config, "steps": args.warmup + args.steps,
+                          "e2_sc": float(energies.e2mp[0, 0]), "e2_pc": float(energies.e2en[0, 0])}), flush=True)
+        return
     # bamat alone, for the roofline (same stream)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
 

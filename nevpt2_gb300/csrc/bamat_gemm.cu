@@ -15,7 +15,8 @@
 //   atmat(ap,bp,cp,a,b,c) += -T3' - (T1 - T2)[b <-> bp]
 // Everything else of the reference loop -- the one-electron terms, the
 // eee2/ee2 terms of the ie loop and the Kronecker-delta pieces of e1t, e2t and
-// eeeet -- is lower order and computed per output element by k_bamat_rest.
+// eeeet -- is lower order; it is evaluated as n^8 GEMMs plus n^7 per-element
+// sums (bamat_rest below).
 // The slabs are materialised from the packed 4-RDM (ord8 gathers, delta
 // corrections of eeee) in the four K-major layouts the GEMMs read.
 #include "nvpt2_internal.h"
@@ -73,62 +74,173 @@ __global__ void k_bamat_ints(const double *atwo, int n, double *A1, double *A2, 
     A3[t] = ATWO(q2 + 1, r3 + 1, s4 + 1, p1 + 1);
 }
 
-// Lower-order terms of the reference loop for one output element (all but
-// the eeee(...) products that the GEMMs cover).  Mirrors k_bamat_direct.
-__global__ void __launch_bounds__(128) k_bamat_rest(Rdm r, const double *atwo, const double *f, int ncore,
-                                                    double *amat, double *atmat) {
-    const int n = r.n, M = r.M;
+// ---------------------------------------------------------------------------
+// Lower-order terms (everything of the reference loop but the eeee products).
+//
+// With the three-operator products materialised once per state,
+//   E2[cp,ap,x3,x4,x5,x6]  = eee2(cp,ap,x3,x4,x5,x6)   (n^6)
+//   E2t[cp,ap,x3,x4,x5,x6] = eee2t(cp,ap,x3,x4,x5,x6)  (n^6)
+//   EE2[cp,ap,x3,x4]       = ee2(cp,ap,x3,x4)          (n^4)
+// and K(x,y) = sum_z atwo(x,z,z,y), f the active block of f(*),
+// Fm = f - K/2, Fp = f + K/2, the ie/ief sums of the loop collapse to
+//   amat  = sum_d [E2[cp,ap,bp,b,d,c] Fm(d,a) - E2[cp,ap,bp,b,a,d] Fp(c,d)
+//                  - E2[cp,ap,bp,d,a,c] Fm(b,d)] + T[cp,ap,bp,b,c,a]
+//   atmat = sum_d [E2t[cp,ap,bp,b,d,c] f(d,a) - E2t[cp,ap,bp,b,a,d] f(c,d)
+//                  + E2t[cp,ap,bp,d,a,c] Fp(b,d) + E2[cp,ap,b,bp,d,c] K(d,a)/2
+//                  + E2[cp,ap,b,bp,a,d] K(c,d)/2]
+//           - T[cp,ap,b,bp,c,a] + 2 V[cp,ap,a,c,b,bp] + [b == bp] D[cp,ap,c,a]
+// with the n^8 contractions (GEMMs)
+//   T[cp,ap,bp,b,c,a] = sum_{d,e} E2[cp,ap,bp,b,d,e] atwo(c,e,d,a)
+//   V[cp,ap,a,c,b,bp] = sum_{d,e} E2[cp,ap,d,e,a,c] atwo(d,e,b,bp)
+// and the n^7 delta block
+//   D[cp,ap,c,a] = 2 sum_{d,e} EE2[cp,ap,d,e] atwo(c,e,d,a)
+//                - sum_d EE2[cp,ap,d,c] K(d,a) - sum_d EE2[cp,ap,a,d] K(c,d)
+//                + 2 sum_{d,e,g} (E2[cp,ap,d,e,g,c] atwo(d,e,g,a) - E2[cp,ap,d,e,a,g] atwo(d,e,c,g)).
+// (The reference's loop at src/koopro4QD.F90:4008-4100 sums the same terms
+// element by element.)  All dense tensors keep (cp,ap) as their two fastest
+// indices, so the per-output kernels read them coalesced along ap.
+
+// 0-based row-major offset of X[x3,x4,x5,x6,cp,ap] ("cp,ap last" layout).
+#define RX6(x3, x4, x5, x6) (((((ll)(x3) * n + (x4)) * n + (x5)) * n + (x6)) * n2 + cpap)
+
+__global__ void __launch_bounds__(256) k_rest_dense(Rdm r, int s, double *E2, double *E2t, double *EE2) {
+    const int n = r.n;
+    const ll n4 = (ll)n * n * n * n, n6 = n4 * n * n;
     ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
-    ll n6 = (ll)n * n * n * n * n * n;
     if (t >= n6) return;
     ll x = t;
-    const int ap = (int)(x % n) + 1; x /= n;
-    const int bp = (int)(x % n) + 1; x /= n;
-    const int cp = (int)(x % n) + 1; x /= n;
-    const int a = (int)(x % n) + 1; x /= n;
-    const int b = (int)(x % n) + 1; x /= n;
-    const int c = (int)(x % n) + 1;
-    for (int s = 1; s <= M; ++s) {
-        double A = 0.0, At = 0.0;
-        for (int d = 1; d <= n; ++d) {
-            double fda = FF(d, a), fcd = FF(c, d), fbd = FF(b, d);
-            A += fda * r.eee2(cp, ap, bp, b, d, c, s) - fcd * r.eee2(cp, ap, bp, b, a, d, s) -
-                 fbd * r.eee2(cp, ap, bp, d, a, c, s);
-            At += fda * r.eee2t(cp, ap, bp, b, d, c, s) - fcd * r.eee2t(cp, ap, bp, b, a, d, s) +
-                  fbd * r.eee2t(cp, ap, bp, d, a, c, s);
-            for (int ie = 1; ie <= n; ++ie) {
-                double dint1 = ATWO(c, ie, d, a), dint2 = ATWO(d, ie, ie, a);
-                double dint3 = ATWO(c, d, d, ie), dint4 = ATWO(b, d, d, ie);
-                double dum1 = r.eee2(cp, ap, bp, b, d, ie, s);
-                double dum2 = r.eee2(cp, ap, bp, b, d, c, s);
-                double dum3 = r.eee2(cp, ap, bp, b, a, ie, s);
-                double dum4 = r.eee2(cp, ap, bp, ie, a, c, s);
-                A += dum1 * dint1 - 0.5 * (dum2 * dint2 + dum3 * dint3 - dum4 * dint4);
-                At += 0.5 * r.eee2t(cp, ap, bp, ie, a, c, s) * dint4;
-                double m1 = -r.eee2(cp, ap, b, bp, d, ie, s);
-                double m2 = -r.eee2(cp, ap, b, bp, d, c, s);
-                double m3 = -r.eee2(cp, ap, b, bp, a, ie, s);
-                if (b == bp) {
-                    m1 += 2.0 * r.ee2(cp, ap, d, ie, s);
-                    m2 += 2.0 * r.ee2(cp, ap, d, c, s);
-                    m3 += 2.0 * r.ee2(cp, ap, a, ie, s);
-                }
-                At += m1 * dint1 - 0.5 * (m2 * dint2 + m3 * dint3);
-                // delta piece of eeeet(cp,ap,bp,ie,d,ief,a,c): [bp == ie] 2 eee2(cp,ap,d,ief,a,c)
-                if (ie == bp)
-                    for (int ief = 1; ief <= n; ++ief)
-                        At += 2.0 * r.eee2(cp, ap, d, ief, a, c, s) * ATWO(d, ief, b, ie);
-                // delta pieces of the mirrored e1t / e2t: [b == bp] 2 eee2(...)
-                if (b == bp)
-                    for (int ief = 1; ief <= n; ++ief)
-                        At += 2.0 * r.eee2(cp, ap, d, ief, ie, c, s) * ATWO(d, ief, ie, a) -
-                              2.0 * r.eee2(cp, ap, d, ief, a, ie, s) * ATWO(d, ief, c, ie);
-            }
-        }
-        ll o = (s - 1) + (ll)M * t;
-        amat[o] = A;
-        atmat[o] = At;
+    const int ap = (int)(x % n); x /= n;
+    const int cp = (int)(x % n); x /= n;
+    const int x6 = (int)(x % n); x /= n;
+    const int x5 = (int)(x % n); x /= n;
+    const int x4 = (int)(x % n); x /= n;
+    const int x3 = (int)x;
+    E2[t] = r.eee2(cp + 1, ap + 1, x3 + 1, x4 + 1, x5 + 1, x6 + 1, s + 1);
+    E2t[t] = r.eee2t(cp + 1, ap + 1, x3 + 1, x4 + 1, x5 + 1, x6 + 1, s + 1);
+    // for t < n^4 the decode gives x3 = x4 = 0 and (x5, x6, cp, ap) = EE2 layout
+    if (t < n4) EE2[t] = r.ee2(cp + 1, ap + 1, x5 + 1, x6 + 1, s + 1);
+}
+
+// Small operands: Fs = [f | K | Fm | Fp] (4 n x n, row-major [x][y]),
+// G[(d,e),(c,a)] = atwo(c,e,d,a) and H[(d,e),(b,bp)] = atwo(d,e,b,bp).
+__global__ void k_rest_ints(const double *atwo, const double *f, int ncore, int n, double *Fs, double *G,
+                            double *H) {
+    ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+    const ll n2 = (ll)n * n, n4 = n2 * n2;
+    if (t >= n4) return;
+    ll x = t;
+    const int q4 = (int)(x % n); x /= n;
+    const int q3 = (int)(x % n); x /= n;
+    const int q2 = (int)(x % n); x /= n;
+    const int q1 = (int)x;
+    // t = ((q1*n + q2)*n + q3)*n + q4
+    G[t] = ATWO(q3 + 1, q2 + 1, q1 + 1, q4 + 1);  // (d,e)=(q1,q2), (c,a)=(q3,q4)
+    H[t] = ATWO(q1 + 1, q2 + 1, q3 + 1, q4 + 1);  // (d,e)=(q1,q2), (b,bp)=(q3,q4)
+    if (t < n2) {
+        const int i = (int)(t / n), j = (int)(t % n);
+        double k = 0.0;
+        for (int z = 1; z <= n; ++z) k += ATWO(i + 1, z, z, j + 1);
+        const double fij = FF(i + 1, j + 1);
+        Fs[t] = fij;
+        Fs[n2 + t] = k;
+        Fs[2 * n2 + t] = fij - 0.5 * k;
+        Fs[3 * n2 + t] = fij + 0.5 * k;
     }
+}
+
+// D[c,a,cp,ap] (n^4 outputs, ap fastest).  U = the EE2 x atwo GEMM, same layout.
+__global__ void __launch_bounds__(256) k_rest_delta(int n, const double *atwo, const double *Fs, const double *E2,
+                                                    const double *EE2, const double *U, double *D) {
+    const ll n2 = (ll)n * n, n4 = n2 * n2;
+    ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n4) return;
+    const ll cpap = t % n2;
+    const int a = (int)((t / n2) % n), c = (int)(t / (n2 * n));
+    const double *K = Fs + n2;
+    double acc = 2.0 * U[t];
+    for (int d = 0; d < n; ++d)
+        acc -= EE2[((ll)d * n + c) * n2 + cpap] * K[d * n + a] + EE2[((ll)a * n + d) * n2 + cpap] * K[c * n + d];
+    double p = 0.0;
+    for (int d = 0; d < n; ++d)
+        for (int e = 0; e < n; ++e)
+            for (int g = 0; g < n; ++g)
+                p += E2[RX6(d, e, g, c)] * ATWO(d + 1, e + 1, g + 1, a + 1) -
+                     E2[RX6(d, e, a, g)] * ATWO(d + 1, e + 1, c + 1, g + 1);
+    D[t] = acc + 2.0 * p;
+}
+
+// Writes amat/atmat(s, ap,bp,cp,a,b,c) (=, not +=) with the lower-order terms.
+__global__ void __launch_bounds__(256) k_rest_out(int n, int M, int s, const double *Fs, const double *E2,
+                                                  const double *E2t, const double *T, const double *V,
+                                                  const double *D, double *amat, double *atmat) {
+    __shared__ double sF[4 * 16 * 16];
+    const ll n2 = (ll)n * n, n4 = n2 * n2;
+    for (int i = threadIdx.x; i < 4 * n2; i += blockDim.x) sF[i] = Fs[i];
+    __syncthreads();
+    ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+    const ll n6 = n4 * n2;
+    if (t >= n6) return;
+    ll x = t;
+    const int ap = (int)(x % n); x /= n;
+    const int bp = (int)(x % n); x /= n;
+    const int cp = (int)(x % n); x /= n;
+    const int a = (int)(x % n); x /= n;
+    const int b = (int)(x % n); x /= n;
+    const int c = (int)x;
+    const ll cpap = (ll)cp * n + ap;
+    const double *f = sF, *K = sF + n2, *Fm = sF + 2 * n2, *Fp = sF + 3 * n2;
+    double A = 0.0, At = 0.0;
+    for (int d = 0; d < n; ++d) {
+        A += E2[RX6(bp, b, d, c)] * Fm[d * n + a] - E2[RX6(bp, b, a, d)] * Fp[c * n + d] -
+             E2[RX6(bp, d, a, c)] * Fm[b * n + d];
+        At += E2t[RX6(bp, b, d, c)] * f[d * n + a] - E2t[RX6(bp, b, a, d)] * f[c * n + d] +
+              E2t[RX6(bp, d, a, c)] * Fp[b * n + d] +
+              0.5 * (E2[RX6(b, bp, d, c)] * K[d * n + a] + E2[RX6(b, bp, a, d)] * K[c * n + d]);
+    }
+    A += T[RX6(bp, b, c, a)];
+    At += 2.0 * V[RX6(b, bp, a, c)] - T[RX6(b, bp, c, a)];
+    if (b == bp) At += D[((ll)c * n + a) * n2 + cpap];
+    const ll o = s + (ll)M * t;
+    amat[o] = A;
+    atmat[o] = At;
+}
+#undef RX6
+
+// row-major C[m,nn] = A^T B with A [k,m] and B [k,nn] row-major (batched over
+// B and C with the given strides; A shared).
+static int dgemm_rm_tA(cublasHandle_t h, long long m, long long nn, long long k, const double *A, const double *B,
+                       long long strideB, double *C, long long strideC, int batch) {
+    const double one = 1.0, zero = 0.0;
+    if (batch == 1)
+        return (int)cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_T, (int)nn, (int)m, (int)k, &one, B, (int)nn, A, (int)m,
+                                &zero, C, (int)nn);
+    return (int)cublasDgemmStridedBatched(h, CUBLAS_OP_N, CUBLAS_OP_T, (int)nn, (int)m, (int)k, &one, B, (int)nn,
+                                          strideB, A, (int)m, 0, &zero, C, (int)nn, strideC, batch);
+}
+
+// Lower-order part of bamat for state s into amat/atmat; scratch holds
+// 4 n^6 + 5 n^4 + 4 n^2 doubles.
+static int bamat_rest(cublasHandle_t h, const Rdm &r, int s, const double *atwo, const double *f, int ncore,
+                      double *amat, double *atmat, double *scratch, cudaStream_t st) {
+    const int n = r.n, M = r.M;
+    const ll n2 = (ll)n * n, n4 = n2 * n2, n6 = n4 * n2;
+    double *E2 = scratch, *E2t = E2 + n6, *T = E2t + n6, *V = T + n6;
+    double *EE2 = V + n6, *U = EE2 + n4, *D = U + n4, *G = D + n4, *H = G + n4, *Fs = H + n4;
+    k_rest_dense<<<(unsigned)((n6 + 255) / 256), 256, 0, st>>>(r, s, E2, E2t, EE2);
+    k_rest_ints<<<(unsigned)((n4 + 255) / 256), 256, 0, st>>>(atwo, f, ncore, n, Fs, G, H);
+    g_launches.fetch_add(2, std::memory_order_relaxed);
+    int rc = 0;
+    // T[(bp,b)][(c,a),(cp,ap)] = G^T E2[(bp,b)][(d,e),(cp,ap)]
+    rc |= dgemm_rm_tA(h, n2, n2, n2, G, E2, n4, T, n4, (int)n2);
+    // V[(b,bp),(a,c,cp,ap)] = H^T E2[(d,e),(a,c,cp,ap)]
+    rc |= dgemm_rm_tA(h, n2, n4, n2, H, E2, 0, V, 0, 1);
+    // U[(c,a),(cp,ap)] = G^T EE2[(d,e),(cp,ap)]
+    rc |= dgemm_rm_tA(h, n2, n2, n2, G, EE2, 0, U, 0, 1);
+    if (rc) return rc;
+    k_rest_delta<<<(unsigned)((n4 + 255) / 256), 256, 0, st>>>(n, atwo, Fs, E2, EE2, U, D);
+    k_rest_out<<<(unsigned)((n6 + 255) / 256), 256, 0, st>>>(n, M, s, Fs, E2, E2t, T, V, D, amat, atmat);
+    g_launches.fetch_add(2, std::memory_order_relaxed);
+    return 0;
 }
 
 // Add the GEMM results: Tk are [(cp,ap) slab][rows][n] with the row layouts
@@ -185,8 +297,15 @@ int launch_bamat_gemm(const Rdm &r, const double *atwo, const double *f, int nco
     if (cublasSetStream(handle.h, st) != CUBLAS_STATUS_SUCCESS) return 1;
     cublasSetMathMode(handle.h, CUBLAS_DEFAULT_MATH);
     // lower-order part first (writes amat/atmat), then add the GEMM terms
-    k_bamat_rest<<<(unsigned)((n6 + 127) / 128), 128, 0, st>>>(r, atwo, f, ncore, amat, atmat);
-    g_launches.fetch_add(1, std::memory_order_relaxed);
+    {
+        double *scr;
+        const ll n2 = (ll)n * n;
+        if (cudaMallocAsync((void **)&scr, sizeof(double) * (4 * n6 + 5 * n4 + 4 * n2), st) != cudaSuccess) return 2;
+        int rrc = 0;
+        for (int s = 0; s < M && !rrc; ++s) rrc = bamat_rest(handle.h, r, s, atwo, f, ncore, amat, atmat, scr, st);
+        cudaFreeAsync(scr, st);
+        if (rrc) return 3;
+    }
     double *A1, *A2, *A3, *T, *X;
     const int B = slabs_per_batch;
     if (cudaMallocAsync((void **)&A1, sizeof(double) * 3 * n4, st) != cudaSuccess) return 2;

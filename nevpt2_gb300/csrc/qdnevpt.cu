@@ -17,6 +17,8 @@
 #include <functional>
 #include <map>
 #include <memory>
+#include <thread>
+#include <exception>
 #include <vector>
 
 #include "../../include/nvpt2.h"
@@ -386,6 +388,18 @@ struct Accum {  // host mirror of the reference's energy holders
           psien(m), nnew(10 * m, -1) {}
     double &E(std::vector<double> &v, int cls, int s) { return v[cls + 8 * s]; }   // (8, M) column-major
     double &H(std::vector<double> &v, int j, int s) { return v[j + M * s]; }       // (M, M) column-major
+    // Adds the contributions a class collected in its own (zero-started)
+    // accumulator.  Every slot a class assigns is zero before that class runs,
+    // so adding reproduces the reference's sequence of stores.
+    void merge(const Accum &o) {
+        auto add = [](std::vector<double> &d, const std::vector<double> &x) {
+            for (size_t i = 0; i < d.size(); ++i) d[i] += x[i];
+        };
+        add(e2mpp, o.e2mpp); add(psimpp, o.psimpp); add(e2enp, o.e2enp); add(psienep, o.psienep);
+        add(e2mp, o.e2mp); add(e2en, o.e2en); add(psimp, o.psimp); add(psien, o.psien);
+        for (size_t i = 0; i < nnew.size(); ++i)
+            if (o.nnew[i] != -1) nnew[i] = o.nnew[i];
+    }
 };
 
 class Runner {
@@ -409,6 +423,17 @@ class Runner {
            std::vector<StateData> &sd_, std::vector<PairData> &pd_, Accum &a)
         : c(cc), nc(nc_), na(na_), nv(nv_), norb(nc_ + na_ + nv_), M(M_), Q(Q_), thr(thr_), fro_h(fro), sd(sd_),
           pd(pd_), acc(a) {}
+
+    // A runner for one class of the current state: its own stream/handles and
+    // accumulator, read-only views of b's per-state tensors.
+    Runner(const Runner &b, Ctx &cc, Accum &a)
+        : c(cc), nc(b.nc), na(b.na), nv(b.nv), norb(b.norb), M(b.M), Q(b.Q), thr(b.thr), fro_h(b.fro_h), sd(b.sd),
+          pd(b.pd), acc(a), s(b.s), eps(b.eps) {
+        B = T::view(b.B); h = T::view(b.h);
+        Rcc = T::view(b.Rcc); Rca = T::view(b.Rca); Rcv = T::view(b.Rcv); Raa = T::view(b.Raa);
+        Rav = T::view(b.Rav); hcv = T::view(b.hcv); hca = T::view(b.hca); hav = T::view(b.hav);
+        Jcc = T::view(b.Jcc);
+    }
 
     bool frozen(int orb) const { return fro_h && fro_h[orb]; }
     std::vector<int> others() const {
@@ -1367,6 +1392,35 @@ T fortran_slice(Ctx &c, const T &F, long long P, long long slot, int n, int k) {
     return out;
 }
 
+// One non-blocking stream with its own cuBLAS/cuSOLVER handles per class,
+// plus the events that order them against the caller's stream.
+struct ClassStreams {
+    std::vector<Ctx> c;
+    std::vector<cudaEvent_t> done;
+    cudaEvent_t prep = nullptr;
+    explicit ClassStreams(size_t n) : c(n, Ctx{nullptr, nullptr, nullptr}), done(n, nullptr) {
+        ck(cudaEventCreateWithFlags(&prep, cudaEventDisableTiming), "cudaEventCreate");
+        for (size_t k = 0; k < n; ++k) {
+            ck(cudaStreamCreateWithFlags(&c[k].st, cudaStreamNonBlocking), "cudaStreamCreate");
+            ck(cudaEventCreateWithFlags(&done[k], cudaEventDisableTiming), "cudaEventCreate");
+            ck(cublasCreate(&c[k].blas), "cublasCreate");
+            ck(cublasSetStream(c[k].blas, c[k].st), "cublasSetStream");
+            ck(cusolverDnCreate(&c[k].sol), "cusolverDnCreate");
+            ck(cusolverDnSetStream(c[k].sol, c[k].st), "cusolverDnSetStream");
+        }
+    }
+    ~ClassStreams() {
+        for (size_t k = 0; k < c.size(); ++k) {
+            if (c[k].st) cudaStreamSynchronize(c[k].st);
+            if (c[k].blas) cublasDestroy(c[k].blas);
+            if (c[k].sol) cusolverDnDestroy(c[k].sol);
+            if (done[k]) cudaEventDestroy(done[k]);
+            if (c[k].st) cudaStreamDestroy(c[k].st);
+        }
+        if (prep) cudaEventDestroy(prep);
+    }
+};
+
 int run_qdnevpt(nvpt_context *ctx, cudaStream_t st, const nvpt_qdnevpt_in *in, nvpt_qdnevpt_out *out,
                 bool on_device, std::string &err) {
     const int nc = (int)in->ncore, na = (int)in->nact, nv = (int)in->nvirt, M = (int)in->metat;
@@ -1464,17 +1518,49 @@ int run_qdnevpt(nvpt_context *ctx, cudaStream_t st, const nvpt_qdnevpt_in *in, n
     bool pc = !in->no_pc;
     std::vector<double> epsnew((size_t)norb * M, 0.0);
     unsigned m = (unsigned)in->class_mask;
+    // The classes of one state only read the state's orbitals and integrals,
+    // so each runs on its own stream, handles and host thread; their
+    // accumulators are merged afterwards in the reference's class order
+    // (0, +1, -1, +2, -2, 0', -1', +1').
+    using Job = std::function<void(Runner &)>;
+    std::vector<Job> jobs;
+    if (m & 1u) jobs.push_back([](Runner &r) { r.class0(); });
+    if (m & 2u) jobs.push_back([pc](Runner &r) { r.class_pm1(true, pc); });
+    if (m & 4u) jobs.push_back([pc](Runner &r) { r.class_pm1(false, pc); });
+    if (m & 8u) jobs.push_back([pc](Runner &r) { r.class_pm2(true, pc); });
+    if (m & 16u) jobs.push_back([pc](Runner &r) { r.class_pm2(false, pc); });
+    if (m & 128u) jobs.push_back([pc](Runner &r) { r.class0p(pc); });
+    if (m & 64u) jobs.push_back([pc](Runner &r) { r.class_pm1p(true, pc); });
+    if (m & 32u) jobs.push_back([pc](Runner &r) { r.class_pm1p(false, pc); });
+    const size_t nj = jobs.size();
+    ClassStreams cs(nj);
     for (int s = 0; s < M; ++s) {
         R.prepare_state(s);
         for (int k = 0; k < norb; ++k) epsnew[k + (size_t)norb * s] = R.eps[k];
-        if (m & 1u) R.class0();
-        if (m & 2u) R.class_pm1(true, pc);
-        if (m & 4u) R.class_pm1(false, pc);
-        if (m & 8u) R.class_pm2(true, pc);
-        if (m & 16u) R.class_pm2(false, pc);
-        if (m & 128u) R.class0p(pc);
-        if (m & 64u) R.class_pm1p(true, pc);
-        if (m & 32u) R.class_pm1p(false, pc);
+        ck(cudaEventRecord(cs.prep, c.st), "event");
+        std::vector<Accum> local(nj, Accum(M));
+        std::vector<std::exception_ptr> fail(nj);
+        int dev = 0;
+        ck(cudaGetDevice(&dev), "cudaGetDevice");
+        auto work = [&](size_t k) {
+            try {
+                ck(cudaSetDevice(dev), "cudaSetDevice");
+                ck(cudaStreamWaitEvent(cs.c[k].st, cs.prep, 0), "wait");
+                Runner W(R, cs.c[k], local[k]);
+                jobs[k](W);
+            } catch (...) {
+                fail[k] = std::current_exception();
+            }
+            cudaEventRecord(cs.done[k], cs.c[k].st);
+        };
+        std::vector<std::thread> th;
+        for (size_t k = 1; k < nj; ++k) th.emplace_back(work, k);
+        if (nj) work(0);
+        for (auto &t : th) t.join();
+        for (size_t k = 0; k < nj; ++k) ck(cudaStreamWaitEvent(c.st, cs.done[k], 0), "wait");
+        for (size_t k = 0; k < nj; ++k)
+            if (fail[k]) std::rethrow_exception(fail[k]);
+        for (size_t k = 0; k < nj; ++k) acc.merge(local[k]);
     }
     ck(cudaStreamSynchronize(c.st), "qdnevpt sync");
     auto put = [](double *dst, const std::vector<double> &v) {

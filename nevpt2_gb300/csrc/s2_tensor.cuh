@@ -36,25 +36,32 @@ inline void ck(cusolverStatus_t e, const char *what) {
     if (e != CUSOLVER_STATUS_SUCCESS) throw Error(2, std::string(what) + ": cuSOLVER status " + std::to_string((int)e));
 }
 
-// Owning device tensor (stream-ordered allocation).
+// Owning device tensor (stream-ordered allocation), or a non-owning view of
+// one (T::view) that never frees.
 struct T {
     double *p = nullptr;
     int nd = 0;
     std::array<long long, 6> sh{{1, 1, 1, 1, 1, 1}};
     cudaStream_t st = nullptr;
+    bool own = true;
     T() = default;
     T(const T &) = delete;
     T &operator=(const T &) = delete;
     T(T &&o) noexcept { *this = std::move(o); }
     T &operator=(T &&o) noexcept {
         release();
-        p = o.p; nd = o.nd; sh = o.sh; st = o.st;
+        p = o.p; nd = o.nd; sh = o.sh; st = o.st; own = o.own;
         o.p = nullptr;
         return *this;
     }
     ~T() { release(); }
+    static T view(const T &o) {
+        T v;
+        v.p = o.p; v.nd = o.nd; v.sh = o.sh; v.st = o.st; v.own = false;
+        return v;
+    }
     void release() {
-        if (p) cudaFreeAsync(p, st);
+        if (p && own) cudaFreeAsync(p, st);
         p = nullptr;
     }
     long long size() const {
