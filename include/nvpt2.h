@@ -137,6 +137,23 @@ int nvpt_bdmat_d(nvpt_context *ctx, const double *atwo, double *dmat, double *dt
                  const double *dal, int64_t nact, int64_t ncore, double *f, const double *aj, int64_t metat,
                  void *stream);
 
+/* No-allocation variant of nvpt_bamat_d -- no counterpart in the reference.
+ * Same arguments and results (to rounding: its contractions sum in another
+ * order), for callers that must not allocate device memory during a run:
+ * a driver whose device memory is budgeted up front by another owner of the
+ * pool, or one for which an allocation failure in the middle of a Koopmans
+ * pass is not acceptable.  All scratch is one file-scope device array sized
+ * for nact <= 8 (4n^6 + 7n^4 + n^2 doubles at n = 8, 8.6 MB); larger nact
+ * returns NVPT_EINVAL.  It calls no cudaMalloc/cudaFree and no allocating
+ * library routine.  Its address is looked up once per device on the first
+ * call, which must be made with the context's device current and should
+ * precede any stream capture.  No scratch word has to start at zero.  Calls
+ * that overlap in time share the array and race: serialise them (one stream,
+ * or events). */
+int nvpt_bamat_static_d(nvpt_context *ctx, double *amat, double *atmat, const double *atwo, const double *ro4,
+                        const double *daaa, const double *taa, const double *dal, int64_t nact, int64_t ncore,
+                        double *f, const double *aj, int64_t norb, int64_t metat, int64_t nsym, void *stream);
+
 
 /* ------------------------------------------------------------------ */
 /* Stage 2 (QDnevpt2.x): SC/PC-NEVPT2 energies of every state.          */

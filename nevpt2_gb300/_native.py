@@ -70,6 +70,7 @@ _SIGS = {
     "nvpt_get_aj_atwo_d": ([P, P, I64, I64, I64, P, P, P, I64, P], ctypes.c_int),
     "nvpt_koop_matrices_ctl_d": ([P, I64, I64, I64] + [P] * 14 + [P], ctypes.c_int),
     "nvpt_bamat_d": ([P] + [P] * 7 + [I64, I64, P, P, I64, I64, I64, P], ctypes.c_int),
+    "nvpt_bamat_static_d": ([P] + [P] * 7 + [I64, I64, P, P, I64, I64, I64, P], ctypes.c_int),
     "nvpt_bbmat_d": ([P] + [P] * 6 + [I64, I64, P, P, I64, P], ctypes.c_int),
     "nvpt_bcmat_d": ([P] + [P] * 6 + [I64, I64, P, P, I64, P], ctypes.c_int),
     "nvpt_bdmat_d": ([P] + [P] * 5 + [I64, I64, P, P, I64, P], ctypes.c_int),

@@ -24,6 +24,7 @@
 #include <cublas_v2.h>
 
 #include <algorithm>
+#include <atomic>
 #include <vector>
 
 namespace nvpt {
@@ -355,6 +356,141 @@ int launch_bamat_gemm(const Rdm &r, const double *atwo, const double *f, int nco
     cudaFreeAsync(T, st);
     cudaFreeAsync(A1, st);
     return rc ? 3 : 0;
+}
+
+// ===========================================================================
+// No-allocation variant (nvpt_bamat_static_d).  Same kernels and the same
+// sequence of contractions as launch_bamat_gemm, but every scratch word lives
+// in one file-scope device array and the GEMMs run on k_dgemm_small below
+// instead of cuBLAS (whose handles and workspaces allocate).  One slab is
+// processed at a time and assembled right away, so the scratch is
+//   max(rest: 4n^6 + 5n^4 + 4n^2, slabs: 4n^6 + 7n^4 + n^2)  doubles,
+// 1,077,312 doubles (8.6 MB) at the maximum of 8 active orbitals.  No word of
+// it has to start at zero: every call writes each word before reading it.
+// Calls that overlap in time (two streams, two host threads, or two devices'
+// contexts sharing the module on one device) race on this array.
+
+static __device__ __align__(256) double g_bamat_scratch[kBamatStaticDoubles];
+
+// Row-major C[m,nn] = op(A) B, op(A) = A [m,k] or, with ta, A^T for A [k,m];
+// B [k,nn].  blockIdx.z selects the batch (strides sA, sB, sC).
+__global__ void __launch_bounds__(256) k_dgemm_small(int m, int nn, int k, int ta, const double *A, ll sA,
+                                                     const double *B, ll sB, double *C, ll sC) {
+    __shared__ double As[16][17], Bs[16][17];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    A += (ll)blockIdx.z * sA;
+    B += (ll)blockIdx.z * sB;
+    C += (ll)blockIdx.z * sC;
+    const int row = blockIdx.y * 16 + ty, col = blockIdx.x * 16 + tx;
+    double acc = 0.0;
+    for (int k0 = 0; k0 < k; k0 += 16) {
+        const int ka = k0 + tx, kb = k0 + ty;
+        As[ty][tx] = (row < m && ka < k) ? (ta ? A[(ll)ka * m + row] : A[(ll)row * k + ka]) : 0.0;
+        Bs[ty][tx] = (kb < k && col < nn) ? B[(ll)kb * nn + col] : 0.0;
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < 16; ++q) acc += As[ty][q] * Bs[q][tx];
+        __syncthreads();
+    }
+    if (row < m && col < nn) C[(ll)row * nn + col] = acc;
+}
+
+static void dgemm_small(cudaStream_t st, ll m, ll nn, ll k, bool ta, const double *A, ll sA, const double *B, ll sB,
+                        double *C, ll sC, int batch) {
+    dim3 grid((unsigned)((nn + 15) / 16), (unsigned)((m + 15) / 16), (unsigned)batch);
+    k_dgemm_small<<<grid, dim3(16, 16), 0, st>>>((int)m, (int)nn, (int)k, ta ? 1 : 0, A, sA, B, sB, C, sC);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+
+// slab_cp[i] = i / n, slab_ap[i] = i % n for the n^2 slabs.
+__global__ void k_slab_list(int n, int *cp, int *ap) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n * n) {
+        cp[i] = i / n;
+        ap[i] = i % n;
+    }
+}
+
+// k_bamat_assemble for the single slab (cp, ap) whose four GEMM results sit
+// at T1..T4 ([n^3 rows][n]).
+__global__ void k_bamat_assemble_slab(int n, int M, int s, int cp, int ap, const double *T1, const double *T2,
+                                      const double *T3, const double *T4, double *amat, double *atmat) {
+    ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+    const ll n4 = (ll)n * n * n * n;
+    if (t >= n4) return;
+    ll x = t;
+    const int bp = (int)(x % n); x /= n;
+    const int a = (int)(x % n); x /= n;
+    const int b = (int)(x % n); x /= n;
+    const int c = (int)x;
+    auto row3 = [n](int i, int j, int k) { return (((ll)i * n + j) * n + k) * n; };
+    double t1 = T1[row3(bp, b, c) + a];
+    double t2 = T2[row3(bp, b, a) + c];
+    double t3 = T3[row3(bp, a, c) + b];
+    double t4 = T4[row3(bp, a, c) + b];
+    double u1 = T1[row3(b, bp, c) + a];
+    double u2 = T2[row3(b, bp, a) + c];
+    const ll o = s + (ll)M * (ap + (ll)n * (bp + (ll)n * (cp + (ll)n * (a + (ll)n * (b + (ll)n * c)))));
+    amat[o] += t1 - t2 - t3;
+    atmat[o] += -t4 - (u1 - u2);
+}
+
+double *bamat_static_scratch(int device) {
+    // One lookup per device, made with that device current (the caller's
+    // first call on it).
+    static std::atomic<double *> addr[64];
+    if (device < 0 || device >= 64) return nullptr;
+    double *p = addr[device].load(std::memory_order_acquire);
+    if (!p) {
+        int cur = -1;
+        if (cudaGetDevice(&cur) != cudaSuccess || cur != device) return nullptr;
+        void *q = nullptr;
+        if (cudaGetSymbolAddress(&q, g_bamat_scratch) != cudaSuccess) return nullptr;
+        p = (double *)q;
+        addr[device].store(p, std::memory_order_release);
+    }
+    return p;
+}
+
+int launch_bamat_static(const Rdm &r, const double *atwo, const double *f, int ncore, double *amat, double *atmat,
+                        cudaStream_t st, double *scratch) {
+    const int n = r.n, M = r.M;
+    if (n > kBamatStaticNactMax) return 1;
+    const ll n2 = (ll)n * n, n3 = n2 * n, n4 = n2 * n2, n6 = n4 * n2;
+    for (int s = 0; s < M; ++s) {
+        // lower-order terms (bamat_rest with the small GEMM kernel)
+        double *E2 = scratch, *E2t = E2 + n6, *T = E2t + n6, *V = T + n6;
+        double *EE2 = V + n6, *U = EE2 + n4, *D = U + n4, *G = D + n4, *H = G + n4, *Fs = H + n4;
+        k_rest_dense<<<(unsigned)((n6 + 255) / 256), 256, 0, st>>>(r, s, E2, E2t, EE2);
+        k_rest_ints<<<(unsigned)((n4 + 255) / 256), 256, 0, st>>>(atwo, f, ncore, n, Fs, G, H);
+        g_launches.fetch_add(2, std::memory_order_relaxed);
+        dgemm_small(st, n2, n2, n2, true, G, 0, E2, n4, T, n4, (int)n2);
+        dgemm_small(st, n2, n4, n2, true, H, 0, E2, 0, V, 0, 1);
+        dgemm_small(st, n2, n2, n2, true, G, 0, EE2, 0, U, 0, 1);
+        k_rest_delta<<<(unsigned)((n4 + 255) / 256), 256, 0, st>>>(n, atwo, Fs, E2, EE2, U, D);
+        k_rest_out<<<(unsigned)((n6 + 255) / 256), 256, 0, st>>>(n, M, s, Fs, E2, E2t, T, V, D, amat, atmat);
+        g_launches.fetch_add(2, std::memory_order_relaxed);
+        // n^9 part, one slab at a time (the same scratch, reused in stream order)
+        double *A1 = scratch, *A2 = A1 + n4, *A3 = A2 + n4;
+        double *T1 = A3 + n4, *T2 = T1 + n4, *T3 = T2 + n4, *T4 = T3 + n4;
+        double *X1 = T4 + n4, *X2 = X1 + n6, *X3 = X2 + n6, *X4 = X3 + n6;
+        int *cpl = (int *)(X4 + n6), *apl = cpl + n2;
+        k_bamat_ints<<<(unsigned)((n4 + 255) / 256), 256, 0, st>>>(atwo, n, A1, A2, A3);
+        k_slab_list<<<(unsigned)((n2 + 255) / 256), 256, 0, st>>>(n, cpl, apl);
+        g_launches.fetch_add(2, std::memory_order_relaxed);
+        for (int sl = 0; sl < n2; ++sl) {
+            k_bamat_slabs<<<(unsigned)((n6 + 255) / 256), 256, 0, st>>>(r, s, cpl + sl, apl + sl, 1, X1, X2, X3, X4);
+            g_launches.fetch_add(1, std::memory_order_relaxed);
+            dgemm_small(st, n3, n, n3, false, X1, 0, A1, 0, T1, 0, 1);
+            dgemm_small(st, n3, n, n3, false, X2, 0, A2, 0, T2, 0, 1);
+            dgemm_small(st, n3, n, n3, false, X3, 0, A3, 0, T3, 0, 1);
+            dgemm_small(st, n3, n, n3, false, X4, 0, A3, 0, T4, 0, 1);
+            k_bamat_assemble_slab<<<(unsigned)((n4 + 255) / 256), 256, 0, st>>>(n, M, s, sl / n, sl % n, T1, T2, T3,
+                                                                                T4, amat, atmat);
+            g_launches.fetch_add(1, std::memory_order_relaxed);
+        }
+    }
+    return 0;
 }
 
 }  // namespace nvpt

@@ -295,6 +295,27 @@ int nvpt_bamat_d(nvpt_context *ctx, double *amat, double *atmat, const double *a
     return after_launch(ctx, "bamat");
 }
 
+int nvpt_bamat_static_d(nvpt_context *ctx, double *amat, double *atmat, const double *atwo, const double *ro4,
+                        const double *daaa, const double *taa, const double *dal, int64_t nact, int64_t ncore,
+                        double *f, const double *aj, int64_t norb, int64_t metat, int64_t nsym, void *stream) {
+    NV_TRY(check_nact(ctx, nact, metat));
+    if (nact > kBamatStaticNactMax)
+        return fail(ctx, NVPT_EINVAL,
+                    "bamat_static: nact=" + std::to_string(nact) + " exceeds the static scratch limit of " +
+                        std::to_string(kBamatStaticNactMax) + " active orbitals; use nvpt_bamat_d");
+    if (nsym != 1) return fail(ctx, NVPT_ENOTSUP, "bamat: only the C1 (nsym=1) path is implemented");
+    if (norb < ncore + nact) return fail(ctx, NVPT_EINVAL, "bamat: norb < ncore+nact");
+    double *scr = bamat_static_scratch(ctx->device);
+    if (!scr)
+        return fail(ctx, NVPT_ECUDA, "bamat_static: scratch address lookup failed (the context's device must be "
+                                     "current on the first call)");
+    cudaStream_t st = pick(ctx, stream);
+    Rdm r = make_rdm(nact, metat, dal, taa, daaa, ro4);
+    launch_build_f(f, aj, atwo, (int)nact, (int)ncore, 1, st);
+    launch_bamat_static(r, atwo, f, (int)ncore, amat, atmat, st, scr);
+    return after_launch(ctx, "bamat_static");
+}
+
 int nvpt_bbmat_d(nvpt_context *ctx, const double *atwo, double *bmat, double *btmat, const double *daaa,
                  const double *taa, const double *dal, int64_t nact, int64_t ncore, double *f, const double *aj,
                  int64_t metat, void *stream) {

@@ -35,6 +35,14 @@ void launch_bamat_direct(const Rdm &r, const double *atwo, const double *f, int 
 // Dense-contraction A-matrix builder (bamat_gemm.cu); 0 on success.
 int launch_bamat_gemm(const Rdm &r, const double *atwo, const double *f, int ncore, double *amat, double *atmat,
                       cudaStream_t st, int slabs_per_batch);
+// No-allocation A-matrix builder (bamat_gemm.cu): scratch in a static device
+// array sized for kBamatStaticNactMax active orbitals; 0 on success, 1 if
+// nact exceeds the limit.
+constexpr int kBamatStaticNactMax = 8;
+constexpr long long kBamatStaticDoubles = 4LL * 262144 + 7LL * 4096 + 64;  // 4n^6 + 7n^4 + n^2 at n = 8
+double *bamat_static_scratch(int device);
+int launch_bamat_static(const Rdm &r, const double *atwo, const double *f, int ncore, double *amat, double *atmat,
+                        cudaStream_t st, double *scratch);
 void launch_ord8(const int64_t *in8, int64_t *out8, int64_t *lindex, long long count, cudaStream_t st);
 
 }  // namespace nvpt
