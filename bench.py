@@ -45,6 +45,8 @@ def _args():
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the bounded CPU baseline sample")
     ap.add_argument("--profile", action="store_true",
                     help="run only --warmup + --steps device-resident steps, untimed (for ncu launch lists)")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "split"],
+                    help="contraction precision of the --profile steps")
     return ap.parse_args()
 
 
@@ -211,12 +213,23 @@ def fp64_peak(dev) -> float:
     return 2 * 4096 ** 3 / (best * 1e-3) / 1e12
 
 
+def _peaks():
+    try:
+        return json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except (OSError, ValueError):
+        return {}
+
+
 def run_ours(args):
+    import ctypes
+
     import torch
     import torch.distributed as dist
 
     from nevpt2_gb300 import koopro, synth
-    from nevpt2_gb300.pipeline import Stage1
+    from nevpt2_gb300 import qdnevpt as gq
+    from nevpt2_gb300._native import ptr
+    from nevpt2_gb300.pipeline import Stage1, ptr_stream
 
     ws, rank = _dist()
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -227,14 +240,21 @@ def run_ours(args):
     p = synth.config_problem(args.config)
     n, M = p.nact, p.metat
 
-    # ---------------- device-resident timing (value) ----------------
     st = Stage1(p, device=str(dev))
+    ctx = st.ctx
     stream = torch.cuda.Stream(dev)
     flush = torch.empty(512 * 2**20 // 4, dtype=torch.float32, device=dev)
+
     def step():
         st.run(stream)
         return st.stage2(stream)
 
+    def set_mode(mode):
+        ctx.call("nvpt_set_precision", mode)
+        koopro.context().call("nvpt_set_precision", mode)
+
+    if args.profile and args.precision == "split":
+        set_mode(koopro.SPLIT)
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             energies = step()
@@ -247,47 +267,67 @@ def run_ours(args):
         print(json.dumps({"profile": args.config, "steps": args.warmup + args.steps,
                           "e2_sc": float(energies.e2mp[0, 0]), "e2_pc": float(energies.e2en[0, 0])}), flush=True)
         return
-    # bamat alone, for the roofline (same stream)
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
 
-    if ws > 1:
-        dist.barrier()
-    torch.cuda.synchronize(dev)
+    def timed_steps(k):
+        """k steps bracketed by barrier + synchronize; CUDA events per step."""
+        if ws > 1:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(k)]
+        e = None
+        with torch.cuda.stream(stream):
+            for i in range(k):
+                flush.zero_()
+                starts[i].record(stream)
+                e = step()
+                ends[i].record(stream)
+        torch.cuda.synchronize(dev)
+        times = [s_.elapsed_time(e_) for s_, e_ in zip(starts, ends)]
+        ms_ = float(np.mean(times))
+        if ws > 1:
+            t = torch.tensor([ms_], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms_ = float(t.item())
+            dist.barrier()
+        return ms_, times, e
+
+    def bamat_alone():
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        o = st.out
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            ev[0].record(stream)
+            ctx.call("nvpt_bamat_d", ptr(o["amatIP"]), ptr(o["amatEA"]), ptr(st.atwo), ptr(st.ro4), ptr(st.daaa),
+                     ptr(st.taa), ptr(st.dal), n, p.ncore, ptr(st.f), ptr(st.aj), p.norb, M, 1, ptr_stream(stream))
+            ev[1].record(stream)
+        torch.cuda.synchronize(dev)
+        return ev[0].elapsed_time(ev[1])
+
+    # ---------------- FP64 (the drop-in): device-resident timing ----------------
     clocks = Clocks()
     clocks.start()
-    launches0 = st.ctx.launches
-    times = []
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    with torch.cuda.stream(stream):
-        for i in range(args.steps):
-            flush.zero_()
-            starts[i].record(stream)
-            energies = step()
-            ends[i].record(stream)
-    torch.cuda.synchronize(dev)
-    launches = st.ctx.launches - launches0
+    launches0 = ctx.launches
+    ms, times, energies = timed_steps(args.steps)
+    launches = ctx.launches - launches0
     clk = clocks.stop()
-    times = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    ms = float(np.mean(times))
-    if ws > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        dist.barrier()
+    bamat_ms = bamat_alone()
 
-    # bamat kernel alone: CUDA events on the launching stream
+    # ---------------- split precision (Ozaki digits on tcgen05) ----------------
+    set_mode(koopro.SPLIT)
     with torch.cuda.stream(stream):
-        flush.zero_()
-        ev[0].record(stream)
-        from nevpt2_gb300._native import ptr
-        from nevpt2_gb300.pipeline import ptr_stream
-        o = st.out
-        st.ctx.call("nvpt_bamat_d", ptr(o["amatIP"]), ptr(o["amatEA"]), ptr(st.atwo), ptr(st.ro4), ptr(st.daaa),
-                    ptr(st.taa), ptr(st.dal), n, p.ncore, ptr(st.f), ptr(st.aj), p.norb, M, 1, ptr_stream(stream))
-        ev[1].record(stream)
+        step()
     torch.cuda.synchronize(dev)
-    bamat_ms = ev[0].elapsed_time(ev[1])
+    clocks_sp = Clocks()
+    clocks_sp.start()
+    ms_sp, times_sp, e_sp = timed_steps(args.steps)
+    clk_sp = clocks_sp.stop()
+    ctx.call("nvpt_set_profiling", 1)
+    bamat_sp_ms = bamat_alone()
+    oz_ms, oz_n, oz_bytes = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
+    ctx.call("nvpt_profile_read", b"oz_gemm", ctypes.byref(oz_ms), ctypes.byref(oz_n), ctypes.byref(oz_bytes))
+    ctx.call("nvpt_set_profiling", 0)
+    set_mode(koopro.FP64)
 
     # ---------------- end to end through the host API (e2e) ----------------
     pinned = {}
@@ -298,19 +338,22 @@ def run_ours(args):
         pinned[name] = t.numpy().reshape(a.shape, order="F")
     from dataclasses import replace
     pp = replace(p, ro4=pinned["ro4"], oneint=pinned["oneint"], chol=pinned["chol"])
-    from nevpt2_gb300 import qdnevpt as gq
 
-    def e2e_step():
+    def e2e_time(mode):
+        set_mode(mode)
         res = koopro.koopro4QD(pp)
-        return res, gq.qdnevpt(pp, res)
+        gq.qdnevpt(pp, res)  # warm
+        tt = []
+        for _ in range(max(1, min(args.steps, 3))):
+            t0 = time.perf_counter()
+            res = koopro.koopro4QD(pp)
+            gq.qdnevpt(pp, res)
+            tt.append(time.perf_counter() - t0)
+        set_mode(koopro.FP64)
+        return float(np.mean(tt)) / M, res
 
-    e2e_step()  # warm
-    e2e_t = []
-    for _ in range(max(1, min(args.steps, 3))):
-        t0 = time.perf_counter()
-        res, en = e2e_step()
-        e2e_t.append(time.perf_counter() - t0)
-    e2e = float(np.mean(e2e_t)) / M
+    e2e, res = e2e_time(koopro.FP64)
+    e2e_sp, _ = e2e_time(koopro.SPLIT)
     W = p.nwords
     b8 = 8
     # stage-1 host calls (ro4 is sent to bro3 and to bamat) + stage-2 datasets
@@ -321,12 +364,19 @@ def run_ours(args):
     if rank != 0:
         dist.destroy_process_group() if ws > 1 else None
         return
-    # roofline: bamat's algorithmic bytes per launch = 8*(live packed 4-RDM + Gamma3 + atwo + 2 outputs)
-    # bamat: FP64 contraction (slab unpack + cuBLAS DGEMMs); algorithmic flops of
-    # the reference loop 12n^9 + 16n^8 + 12n^7 per state
+    # roofline (FP64 path): bamat as FP64 contractions (slab unpack + cuBLAS
+    # DGEMMs); algorithmic flops of the reference loop 12n^9 + 16n^8 + 12n^7
+    # per state, against the FP64 DGEMM rate measured in this run.
     alg_flops = M * (12 * n**9 + 16 * n**8 + 12 * n**7)
     peak64 = fp64_peak(dev)
     achieved = alg_flops / (bamat_ms * 1e-3) / 1e12
+    # roofline (split path): the Ozaki product kernel streams digit tiles
+    # (9 BF16 digits per FP64 element) from HBM once; algorithmic bytes per
+    # launch = all digits of X and A + the FP64 results.
+    pk = _peaks()
+    hbm_peak = pk.get("hbm_gbs", 6800.0)
+    oz_gbs = oz_bytes.value / (oz_ms.value * 1e-3) / 1e9 if oz_ms.value > 0 else None
+    de = lambda a_, b_: float(np.abs(np.asarray(a_) - np.asarray(b_)).max())
     koop = {k: st.result(k) for k in st.out}
     koop.update({"1-RDM": p.dal, "2-RDM": p.taa, "3-RDM": p.daaa})
     cb = cpu_baseline(p, args.cpu_seconds, koop)
@@ -335,11 +385,25 @@ def run_ours(args):
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded CI vector, exact RDMs, random DF integrals)",
             "config": workload_desc(p), "gpu_launches": int(launches),
             "e2e": {"value": e2e, "unit": "s/state", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-            "roofline": {"kernel": "bamat (k_bamat_slabs + cuBLAS DGEMM + k_bamat_rest)", "bound": "tensor",
+            "roofline": {"kernel": "bamat (k_bamat_slabs + cuBLAS DGEMM + k_rest_*)", "bound": "tensor",
                          "achieved": achieved, "peak": peak64, "unit": "TFLOP/s", "frac": achieved / peak64,
                          "traffic": None, "precision": "fp64",
                          "peak_source": "FP64 DGEMM rate measured live in this run (cuBLAS 4096^3)",
                          "kernel_ms": bamat_ms, "alg_flops": alg_flops},
+            "split": {"value": ms_sp / 1e3 / M, "unit": "s/state", "ms_per_step": ms_sp,
+                      "speedup_vs_fp64": ms / ms_sp, "bamat_ms": bamat_sp_ms, "bamat_speedup": bamat_ms / bamat_sp_ms,
+                      "e2e": {"value": e2e_sp, "unit": "s/state"},
+                      "energy_err_eh": {"per_class_sc_max": de(e_sp.e2mpp, energies.e2mpp),
+                                        "per_class_pc_max": de(e_sp.e2enp, energies.e2enp),
+                                        "total_sc": de(e_sp.e2mp, energies.e2mp),
+                                        "total_pc": de(e_sp.e2en, energies.e2en)},
+                      "nnew_equal": bool(np.array_equal(e_sp.nnew, energies.nnew)),
+                      "roofline": {"kernel": "k_oz_gemm (Ozaki digit products, tcgen05)", "bound": "hbm",
+                                   "achieved": oz_gbs, "peak": hbm_peak, "unit": "GB/s",
+                                   "frac": (oz_gbs / hbm_peak) if oz_gbs else None, "traffic": None,
+                                   "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+                                   "kernel_ms": oz_ms.value, "launches": oz_n.value, "alg_bytes": oz_bytes.value},
+                      "clocks": clk_sp, "step_ms_all": times_sp},
             "energies": {"e2_sc": float(energies.e2mp[0, 0]), "e2_pc": float(energies.e2en[0, 0]),
                          "per_class_sc": [float(x) for x in energies.e2mpp[:, 0]],
                          "per_class_pc": [float(x) for x in energies.e2enp[:, 0]],

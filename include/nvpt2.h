@@ -137,6 +137,34 @@ int nvpt_bdmat_d(nvpt_context *ctx, const double *atwo, double *dmat, double *dt
                  const double *dal, int64_t nact, int64_t ncore, double *f, const double *aj, int64_t metat,
                  void *stream);
 
+/* Precision of the dense contractions of later calls on ctx (no counterpart
+ * in the reference).  NVPT_PRECISION_FP64 (the default) is the drop-in.
+ * NVPT_PRECISION_SPLIT runs the n^9 slab products of bamat as Ozaki digit
+ * products on the tensor cores: each FP64 operand row/column is scaled by a
+ * power of two and cut into nine 6-bit digits held exactly in BF16, every
+ * digit pair with weight >= 2^-60 is summed exactly in FP32, and the partial
+ * products are recombined in FP64 (error below 2^-51 of the row/column
+ * maximum per product).  Eigensolves, pseudo-inverses, denominators and
+ * energy sums always run in FP64. */
+#define NVPT_PRECISION_FP64 0
+#define NVPT_PRECISION_SPLIT 1
+int nvpt_set_precision(nvpt_context *ctx, int precision);
+int nvpt_get_precision(nvpt_context *ctx);
+
+/* Live kernel timing (no counterpart in the reference).  While enabled
+ * (process-wide), tagged launches are bracketed by CUDA events on their
+ * stream; nvpt_profile_read waits for and sums the spans of one tag (total
+ * ms, launch count, algorithmic bytes) and forgets them.  Tags: "oz_gemm"
+ * (the split-precision product kernel). */
+int nvpt_set_profiling(nvpt_context *ctx, int on);
+int nvpt_profile_read(nvpt_context *ctx, const char *tag, double *ms, int64_t *launches, int64_t *bytes);
+
+/* The split-precision product as a building block (no counterpart in the
+ * reference): row-major C[m,n] = A[m,k] B[k,n] on device pointers, with
+ * n <= 16 and k <= 4096 (the exactness limit of the FP32 digit sums). */
+int nvpt_dgemm_split_d(nvpt_context *ctx, int64_t m, int64_t n, int64_t k, const double *A, const double *B,
+                       double *C, void *stream);
+
 /* No-allocation variant of nvpt_bamat_d -- no counterpart in the reference.
  * Same arguments and results (to rounding: its contractions sum in another
  * order), for callers that must not allocate device memory during a run:

@@ -71,6 +71,11 @@ _SIGS = {
     "nvpt_koop_matrices_ctl_d": ([P, I64, I64, I64] + [P] * 14 + [P], ctypes.c_int),
     "nvpt_bamat_d": ([P] + [P] * 7 + [I64, I64, P, P, I64, I64, I64, P], ctypes.c_int),
     "nvpt_bamat_static_d": ([P] + [P] * 7 + [I64, I64, P, P, I64, I64, I64, P], ctypes.c_int),
+    "nvpt_set_precision": ([P, ctypes.c_int], ctypes.c_int),
+    "nvpt_get_precision": ([P], ctypes.c_int),
+    "nvpt_dgemm_split_d": ([P, I64, I64, I64, P, P, P, P], ctypes.c_int),
+    "nvpt_set_profiling": ([P, ctypes.c_int], ctypes.c_int),
+    "nvpt_profile_read": ([P, ctypes.c_char_p, P, P, P], ctypes.c_int),
     "nvpt_bbmat_d": ([P] + [P] * 6 + [I64, I64, P, P, I64, P], ctypes.c_int),
     "nvpt_bcmat_d": ([P] + [P] * 6 + [I64, I64, P, P, I64, P], ctypes.c_int),
     "nvpt_bdmat_d": ([P] + [P] * 5 + [I64, I64, P, P, I64, P], ctypes.c_int),

@@ -20,6 +20,7 @@
 // The slabs are materialised from the packed 4-RDM (ord8 gathers, delta
 // corrections of eeee) in the four K-major layouts the GEMMs read.
 #include "nvpt2_internal.h"
+#include "ozaki.cuh"
 
 #include <cublas_v2.h>
 
@@ -290,7 +291,7 @@ static int dgemm_rm(cublasHandle_t h, long long m, long long nn, long long k, co
 
 // Returns 0 on success, else a CUDA / cuBLAS error code (nonzero).
 int launch_bamat_gemm(const Rdm &r, const double *atwo, const double *f, int ncore, double *amat, double *atmat,
-                      cudaStream_t st, int slabs_per_batch) {
+                      cudaStream_t st, int slabs_per_batch, bool split) {
     const int n = r.n, M = r.M;
     const ll n3 = (ll)n * n * n, n4 = n3 * n, n6 = n3 * n3;
     static thread_local BamatGemm handle;
@@ -329,6 +330,12 @@ int launch_bamat_gemm(const Rdm &r, const double *atwo, const double *f, int nco
         cudaStreamSynchronize(st);
     }
     int rc = 0;
+    // split precision: digit workspace for a full batch of slabs
+    void *ozw = nullptr;
+    if (split) {
+        oz::OzPlan pl(4, (ll)B * n3, (int)n3, n);
+        if (cudaMallocAsync(&ozw, pl.bytes(), st) != cudaSuccess) return 2;
+    }
     for (int s = 0; s < M && !rc; ++s) {
         for (int s0 = 0; s0 < n * n && !rc; s0 += B) {
             int nb = std::min(B, n * n - s0);
@@ -340,6 +347,12 @@ int launch_bamat_gemm(const Rdm &r, const double *atwo, const double *f, int nco
             ll rows = (ll)nb * n3;
             double *T1 = T + (ll)s0 * n4, *T2 = T + n6 + (ll)s0 * n4, *T3 = T + 2 * n6 + (ll)s0 * n4,
                    *T4 = T + 3 * n6 + (ll)s0 * n4;
+            if (split) {
+                const double *Xs[4] = {X1, X2, X3, X4}, *As[4] = {A1, A2, A3, A3};
+                double *Ts[4] = {T1, T2, T3, T4};
+                rc |= oz::oz_gemm_skinny(oz::OzPlan(4, rows, (int)n3, n), Xs, As, Ts, n, n, ozw, st);
+                continue;
+            }
             rc |= dgemm_rm(handle.h, rows, n, n3, X1, A1, T1);
             rc |= dgemm_rm(handle.h, rows, n, n3, X2, A2, T2);
             rc |= dgemm_rm(handle.h, rows, n, n3, X3, A3, T3);
@@ -351,11 +364,16 @@ int launch_bamat_gemm(const Rdm &r, const double *atwo, const double *f, int nco
             g_launches.fetch_add(1, std::memory_order_relaxed);
         }
     }
+    if (ozw) {
+        // the product kernels share one error flag (a wait that timed out)
+        if (!rc && oz::oz_check_error(ozw, st) != 0) rc = 5;
+        cudaFreeAsync(ozw, st);
+    }
     cudaFreeAsync(slabs, st);
     cudaFreeAsync(X, st);
     cudaFreeAsync(T, st);
     cudaFreeAsync(A1, st);
-    return rc ? 3 : 0;
+    return rc == 5 ? 5 : (rc ? 3 : 0);
 }
 
 // ===========================================================================

@@ -4,14 +4,49 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
 #include "../../include/nvpt2.h"
 #include "nvpt2_internal.h"
+#include "ozaki.cuh"
 
 namespace nvpt {
 std::atomic<long long> g_launches{0};
+
+namespace {
+std::atomic<bool> g_prof{false};
+struct ProfRecord {
+    std::string tag;
+    cudaEvent_t a, b;
+    long long bytes;
+};
+std::mutex g_prof_mu;
+std::vector<ProfRecord> g_prof_rec;
+}  // namespace
+
+bool prof_enabled() { return g_prof.load(std::memory_order_relaxed); }
+
+void ProfSpan::begin(const char *t, cudaStream_t s, long long nbytes) {
+    if (!prof_enabled()) return;
+    if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
+        a = b = nullptr;
+        return;
+    }
+    tag = t;
+    st = s;
+    bytes = nbytes;
+    cudaEventRecord(a, s);
+}
+
+void ProfSpan::end() {
+    if (!a) return;
+    cudaEventRecord(b, st);
+    std::lock_guard<std::mutex> g(g_prof_mu);
+    g_prof_rec.push_back(ProfRecord{tag, a, b, bytes});
+    a = b = nullptr;
+}
 
 // src/ord_utils.F90:71 ord8 over a batch of tuples (bit-exactness tests).
 __global__ void k_ord8(const int64_t *in8, int64_t *out8, int64_t *lindex, long long count) {
@@ -45,6 +80,7 @@ using namespace nvpt;
 
 struct nvpt_context {
     int device = 0;
+    int precision = NVPT_PRECISION_FP64;
     cudaStream_t stream = nullptr;
     std::string err;
     long long launches_at_create = 0;
@@ -288,10 +324,12 @@ int nvpt_bamat_d(nvpt_context *ctx, double *amat, double *atmat, const double *a
         launch_bamat_direct(r, atwo, f, (int)ncore, amat, atmat, st);
         return after_launch(ctx, "bamat");
     }
-    int slabs = nact >= 15 ? 2 : 4;
-    int rc = launch_bamat_gemm(r, atwo, f, (int)ncore, amat, atmat, st, slabs);
+    const bool split = ctx->precision == NVPT_PRECISION_SPLIT;
+    int slabs = split ? 16 : (nact >= 15 ? 2 : 4);
+    int rc = launch_bamat_gemm(r, atwo, f, (int)ncore, amat, atmat, st, slabs, split);
     if (rc == 2) return fail(ctx, NVPT_ENOMEM, "bamat: device allocation failed");
-    if (rc) return fail(ctx, NVPT_ECUDA, "bamat: cuBLAS GEMM failed");
+    if (rc == 5) return fail(ctx, NVPT_ETIMEDOUT, "bamat: a split-precision product timed out waiting on its pipeline");
+    if (rc) return fail(ctx, NVPT_ECUDA, split ? "bamat: split-precision product failed" : "bamat: cuBLAS GEMM failed");
     return after_launch(ctx, "bamat");
 }
 
@@ -314,6 +352,70 @@ int nvpt_bamat_static_d(nvpt_context *ctx, double *amat, double *atmat, const do
     launch_build_f(f, aj, atwo, (int)nact, (int)ncore, 1, st);
     launch_bamat_static(r, atwo, f, (int)ncore, amat, atmat, st, scr);
     return after_launch(ctx, "bamat_static");
+}
+
+int nvpt_set_precision(nvpt_context *ctx, int precision) {
+    if (!ctx) return NVPT_EINVAL;
+    if (precision != NVPT_PRECISION_FP64 && precision != NVPT_PRECISION_SPLIT)
+        return fail(ctx, NVPT_EINVAL, "precision must be NVPT_PRECISION_FP64 or NVPT_PRECISION_SPLIT");
+    ctx->precision = precision;
+    return NVPT_OK;
+}
+
+int nvpt_get_precision(nvpt_context *ctx) { return ctx ? ctx->precision : -1; }
+
+int nvpt_set_profiling(nvpt_context *ctx, int on) {
+    if (!ctx) return NVPT_EINVAL;
+    g_prof.store(on != 0);
+    return NVPT_OK;
+}
+
+int nvpt_profile_read(nvpt_context *ctx, const char *tag, double *ms, int64_t *launches, int64_t *bytes) {
+    if (!ctx || !tag) return NVPT_EINVAL;
+    double t = 0.0;
+    int64_t n = 0, by = 0;
+    std::lock_guard<std::mutex> g(g_prof_mu);
+    std::vector<ProfRecord> keep;
+    int rc = NVPT_OK;
+    for (auto &r : g_prof_rec) {
+        if (r.tag != tag) {
+            keep.push_back(r);
+            continue;
+        }
+        float e = 0.f;
+        if (cudaEventSynchronize(r.b) != cudaSuccess || cudaEventElapsedTime(&e, r.a, r.b) != cudaSuccess)
+            rc = NVPT_ECUDA;
+        t += e;
+        ++n;
+        by += r.bytes;
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    g_prof_rec.swap(keep);
+    if (ms) *ms = t;
+    if (launches) *launches = n;
+    if (bytes) *bytes = by;
+    return rc == NVPT_OK ? NVPT_OK : fail(ctx, rc, "profile_read: event query failed");
+}
+
+int nvpt_dgemm_split_d(nvpt_context *ctx, int64_t m, int64_t n, int64_t k, const double *A, const double *B,
+                       double *C, void *stream) {
+    if (!ctx || !A || !B || !C) return NVPT_EINVAL;
+    if (m < 1 || n < 1 || n > 16 || k < 1 || k > 4096)
+        return fail(ctx, NVPT_EINVAL, "dgemm_split: need m >= 1, 1 <= n <= 16, 1 <= k <= 4096");
+    cudaStream_t st = pick(ctx, stream);
+    oz::OzPlan pl(1, m, (int)k, (int)n);
+    void *w = nullptr;
+    NV_TRY(cuda_check(ctx, cudaMallocAsync(&w, pl.bytes(), st), "dgemm_split workspace"));
+    const double *X[1] = {A}, *As[1] = {B};
+    double *T[1] = {C};
+    int rc = oz::oz_gemm_skinny(pl, X, As, T, (int)n, (int)n, w, st);
+    int rc2 = rc ? 0 : oz::oz_check_error(w, st);
+    cudaFreeAsync(w, st);
+    if (rc) return fail(ctx, NVPT_ECUDA, "dgemm_split: launch failed");
+    if (rc2 == 4) return fail(ctx, NVPT_ETIMEDOUT, "dgemm_split: the product timed out waiting on its pipeline");
+    if (rc2) return fail(ctx, NVPT_ECUDA, "dgemm_split: error flag read-back failed");
+    return after_launch(ctx, "dgemm_split");
 }
 
 int nvpt_bbmat_d(nvpt_context *ctx, const double *atwo, double *bmat, double *btmat, const double *daaa,

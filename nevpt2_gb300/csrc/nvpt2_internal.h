@@ -32,9 +32,12 @@ void launch_bdmat(const Rdm &r, const double *atwo, const double *f, const doubl
                   double *dt, cudaStream_t st);
 void launch_bamat_direct(const Rdm &r, const double *atwo, const double *f, int ncore, double *amat, double *atmat,
                          cudaStream_t st);
-// Dense-contraction A-matrix builder (bamat_gemm.cu); 0 on success.
+// Dense-contraction A-matrix builder (bamat_gemm.cu); 0 on success, 2 on a
+// failed allocation, 5 if a split-precision product timed out, else a
+// cuBLAS / launch failure.  split: the n^9 slab products run as Ozaki digit
+// products on the tensor cores (ozaki.cu) instead of FP64 DGEMMs.
 int launch_bamat_gemm(const Rdm &r, const double *atwo, const double *f, int ncore, double *amat, double *atmat,
-                      cudaStream_t st, int slabs_per_batch);
+                      cudaStream_t st, int slabs_per_batch, bool split = false);
 // No-allocation A-matrix builder (bamat_gemm.cu): scratch in a static device
 // array sized for kBamatStaticNactMax active orbitals; 0 on success, 1 if
 // nact exceeds the limit.
@@ -43,6 +46,18 @@ constexpr long long kBamatStaticDoubles = 4LL * 262144 + 7LL * 4096 + 64;  // 4n
 double *bamat_static_scratch(int device);
 int launch_bamat_static(const Rdm &r, const double *atwo, const double *f, int ncore, double *amat, double *atmat,
                         cudaStream_t st, double *scratch);
+// Kernel spans for live measurement (nvpt_set_profiling): when enabled, a
+// tagged launch is bracketed by CUDA events on its stream together with its
+// algorithmic byte count; nvpt_profile_read sums the spans of one tag.
+bool prof_enabled();
+struct ProfSpan {
+    cudaEvent_t a = nullptr, b = nullptr;
+    const char *tag = nullptr;
+    cudaStream_t st = nullptr;
+    long long bytes = 0;
+    void begin(const char *t, cudaStream_t s, long long nbytes);
+    void end();
+};
 void launch_ord8(const int64_t *in8, int64_t *out8, int64_t *lindex, long long count, cudaStream_t st);
 
 }  // namespace nvpt

@@ -1,0 +1,455 @@
+// Split-precision (Ozaki) products T = X A for tall-skinny FP64 operands on
+// the 5th-generation tensor cores: X [rows, K], A [K, ncols <= 16], K <= 4096.
+//
+// Scheme.  Every row i of X is scaled by 2^-E_i (E_i: smallest power of two
+// above max_k |X[i,k]|) and its magnitude truncated to 54 fractional bits,
+// which are cut into NSL = 9 signed 6-bit digits d_p (p = 0 most significant):
+//   X[i,k] ~ 2^E_i sum_p d_p[i,k] 2^-6(p+1),   |d_p| <= 63.
+// Columns of A are split the same way with their own exponents F_j.  Each
+// digit is an exact BF16.  For every digit pair (p,q) with p + q <= 8 the
+// tensor cores form S_pq = sum_k d_p e_q in FP32; |S_pq| <= 63*63*K < 2^24
+// for K <= 4096, so these sums are exact.  The epilogue recombines
+//   T[i,j] = 2^(E_i + F_j - 12) sum_t 2^-6t sum_{p+q=t} S_pq[i,j]
+// in integer and FP64 arithmetic.  The error is the digit truncation (2^-54
+// of the row / column maximum) plus the dropped pairs p + q > 8 (< 2^-51),
+// i.e. about FP64 rounding.
+//
+// Kernel.  One CTA per SM (persistent over 128-row tiles of up to four
+// products), 192 threads: warp 4 streams digit tiles global -> shared with
+// 1-D bulk copies (cp.async.bulk, mbarrier transaction counts), warp 5 issues
+// tcgen05.mma (M = 128, K = 16, N = 16 (9 - p) for the q-slices of slice p,
+// concatenated along N) into TMEM, warps 0-3 read the accumulators back with
+// tcgen05.ld and recombine.  The 45 digit pairs need 720 accumulator columns,
+// so each tile runs two passes over K (slices p < 4 into 480 columns, then
+// p >= 4 into 240); each pass streams only its own digit slices.  The split kernels write
+// the digits directly in the UMMA no-swizzle K-major core-matrix order, so a
+// pipeline stage (KC = 32 columns of K) is one contiguous block in HBM.
+// Every wait is bounded; a timeout sets the error flag and the kernel winds
+// down (waits for its copies in flight, frees TMEM) instead of hanging.
+#include <cstdint>
+
+#include "nvpt2_internal.h"
+#include "ozaki.cuh"
+
+namespace nvpt {
+namespace oz {
+
+constexpr uint32_t kSpinLimit = 1u << 22;  // polls (with ~100 ns back-off) before a wait gives up
+
+// TMEM column of the (p, q = 0) accumulator within p's pass.
+__host__ __device__ constexpr int col_off(int p) {
+    return NB * ((p < PASS_SPLIT ? p : p - PASS_SPLIT) * NSL -
+                 (p * (p - 1) / 2 - (p < PASS_SPLIT ? 0 : PASS_SPLIT * (PASS_SPLIT - 1) / 2)));
+}
+static_assert(col_off(3) + NB * (NSL - 3) <= TMEM_COLS, "pass 0 fits TMEM");
+static_assert(col_off(8) + NB * (NSL - 8) <= TMEM_COLS, "pass 1 fits TMEM");
+
+// ---------------------------------------------------------------- device PTX
+__device__ __forceinline__ uint32_t su32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred P;\n\tmbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n\tselp.u32 %0, 1, 0, P;\n}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait on the phase with the given parity.  Gives up (returning
+// false) when the limit is reached -- setting *err -- or when another role
+// has already set *err.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int *err) {
+    for (uint32_t i = 0; i < kSpinLimit; ++i) {
+        if (mbar_test(bar, parity)) return true;
+        if ((i & 255u) == 255u && *(volatile int *)err) return false;
+        if (i > 1024) __nanosleep(100);
+    }
+    atomicExch(err, 1);
+    return false;
+}
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+// UMMA shared-memory descriptor, no swizzle (start, leading-dim byte offset =
+// next K core matrix, stride byte offset = next 8-row group, version 1).
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+// Instruction descriptor: D f32, A bf16, B bf16, both K-major, M = 128.
+__device__ __forceinline__ uint32_t idesc_bf16(int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+}
+__device__ __forceinline__ void umma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\ttcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// 2^e as a double (normal range).
+__device__ __forceinline__ double pow2(int e) {
+    e = max(-1022, min(1023, e));
+    return __longlong_as_double((long long)(e + 1023) << 52);
+}
+
+// ------------------------------------------------------------- the product
+constexpr int A_ROW = NSL * A_TILE;  // digit bytes of one (row tile, K chunk) in HBM
+
+__global__ void __launch_bounds__(192, 1) k_oz_gemm(OzBatch b, int *err) {
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ __align__(8) uint64_t bar_full[STAGES], bar_empty[STAGES], bar_tfull, bar_tempty, bar_done;
+    __shared__ uint32_t s_tmem;
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const uint32_t sA0 = su32(smem), sB0 = sA0 + STAGES * A_STAGE;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    long long ntiles = 0;
+    for (int j = 0; j < b.njob; ++j) ntiles += b.job[j].nrt;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(su32(&bar_full[s]), 1);
+            mbar_init(su32(&bar_empty[s]), 1);
+        }
+        mbar_init(su32(&bar_tfull), 1);
+        mbar_init(su32(&bar_tempty), 128);
+        mbar_init(su32(&bar_done), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&s_tmem)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = s_tmem;
+
+    auto decode = [&](long long tile, int &j, int &rt) {
+        j = 0;
+        while (tile >= b.job[j].nrt) {
+            tile -= b.job[j].nrt;
+            ++j;
+        }
+        rt = (int)tile;
+    };
+
+    if (warp == 4) {
+        // ---------------- producer: digit tiles global -> shared
+        if (lane == 0) {
+            uint32_t it = 0;
+            bool ok = true;
+            for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+                int j, rt;
+                decode(tile, j, rt);
+                const uint8_t *asrc = b.job[j].ad + (size_t)rt * b.nkc * A_ROW;
+                const uint8_t *bsrc = b.job[j].bd;
+                for (int pass = 0; pass < NPASS && ok; ++pass) {
+                    const uint32_t abytes = (uint32_t)(pass_p0(pass + 1) - pass_p0(pass)) * A_TILE;
+                    for (int kc = 0; kc < b.nkc; ++kc, ++it) {
+                        const uint32_t s = it % STAGES, ph = (it / STAGES) & 1u;
+                        if (!mbar_wait(su32(&bar_empty[s]), ph ^ 1u, err)) {
+                            ok = false;
+                            break;
+                        }
+                        mbar_expect_tx(su32(&bar_full[s]), abytes + B_STAGE);
+                        bulk_g2s(sA0 + s * A_STAGE, asrc + (size_t)kc * A_ROW + (size_t)pass_p0(pass) * A_TILE, abytes,
+                                 su32(&bar_full[s]));
+                        bulk_g2s(sB0 + s * B_STAGE, bsrc + (size_t)kc * B_STAGE, B_STAGE, su32(&bar_full[s]));
+                    }
+                }
+            }
+            // copies still in flight land on the full barriers of the last
+            // STAGES iterations: wait for them (bounded) before exiting
+            const uint32_t first = it > (uint32_t)STAGES ? it - STAGES : 0u;
+            for (uint32_t k = first; k < it; ++k) {
+                const uint32_t s = k % STAGES, ph = (k / STAGES) & 1u;
+                for (uint32_t i = 0; i < kSpinLimit && !mbar_test(su32(&bar_full[s]), ph); ++i) __nanosleep(100);
+            }
+        }
+    } else if (warp == 5) {
+        // ---------------- MMA issuer
+        if (lane == 0) {
+            uint32_t it = 0, tl = 0;
+            bool ok = true;
+            for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+                for (int pass = 0; pass < NPASS && ok; ++pass, ++tl) {
+                    if (!mbar_wait(su32(&bar_tempty), (tl & 1u) ^ 1u, err)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const int p0 = pass_p0(pass), p1 = pass_p0(pass + 1);
+                    for (int kc = 0; kc < b.nkc; ++kc, ++it) {
+                        const uint32_t s = it % STAGES, ph = (it / STAGES) & 1u;
+                        if (!mbar_wait(su32(&bar_full[s]), ph, err)) {
+                            ok = false;
+                            break;
+                        }
+                        tc_fence_after();
+                        const uint32_t a0 = sA0 + s * A_STAGE, b0 = sB0 + s * B_STAGE;
+                        for (int p = p0; p < p1; ++p) {
+                            const uint32_t id = idesc_bf16(NB * (NSL - p));
+#pragma unroll
+                            for (int kk = 0; kk < KC / 16; ++kk) {
+                                const uint64_t da = sdesc(a0 + (p - p0) * A_TILE + kk * 2 * LBO_A, LBO_A, SBO);
+                                const uint64_t db = sdesc(b0 + kk * 2 * LBO_B, LBO_B, SBO);
+                                umma(tmem + (uint32_t)col_off(p), da, db, id, (kc > 0 || kk > 0) ? 1u : 0u);
+                            }
+                        }
+                        umma_commit(su32(&bar_empty[s]));
+                    }
+                    if (ok) umma_commit(su32(&bar_tfull));
+                }
+            }
+            // every MMA this thread issued has finished before TMEM is freed
+            umma_commit(su32(&bar_done));
+            for (uint32_t i = 0; i < kSpinLimit && !mbar_test(su32(&bar_done), 0); ++i) __nanosleep(100);
+        }
+    } else {
+        // ---------------- epilogue (warps 0-3: TMEM lanes 32 w .. 32 w + 31)
+        uint32_t tl = 0;
+        bool ok = true;
+        for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+            int j, rt;
+            decode(tile, j, rt);
+            const OzJob &J = b.job[j];
+            const long long row = (long long)rt * BM + warp * 32 + lane;
+            const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16);
+            double tot[NB];
+#pragma unroll
+            for (int c = 0; c < NB; ++c) tot[c] = 0.0;
+            for (int pass = 0; pass < NPASS; ++pass, ++tl) {
+                const bool got = mbar_wait(su32(&bar_tfull), tl & 1u, err);
+                if (!__all_sync(0xffffffffu, got)) {  // warp-uniform: tcgen05.ld is .sync.aligned
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const int p0 = pass_p0(pass), p1 = pass_p0(pass + 1);
+                double acc[NB];
+#pragma unroll
+                for (int c = 0; c < NB; ++c) acc[c] = 0.0;
+                for (int t = NSL - 1; t >= 0; --t) {  // Horner in 2^-6 over t = p + q
+                    int v[NB];
+#pragma unroll
+                    for (int c = 0; c < NB; ++c) v[c] = 0;
+                    for (int p = p0; p < p1 && p <= t; ++p) {
+                        uint32_t r[16];
+                        tmem_ld16(tbase + (uint32_t)(col_off(p) + NB * (t - p)), r);
+#pragma unroll
+                        for (int c = 0; c < NB; ++c) v[c] += __float2int_rn(__uint_as_float(r[c]));
+                    }
+#pragma unroll
+                    for (int c = 0; c < NB; ++c) acc[c] = fma(acc[c], 1.0 / 64.0, (double)v[c]);
+                }
+#pragma unroll
+                for (int c = 0; c < NB; ++c) tot[c] += acc[c];
+                tc_fence_before();
+                mbar_arrive(su32(&bar_tempty));
+            }
+            if (ok && row < J.rows) {
+                const int ei = J.rexp[row];
+                double *o = J.out + row * b.ldo;
+                for (int c = 0; c < b.ncols; ++c) o[c] = tot[c] * pow2(ei + J.cexp[c] - 12);
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    }
+}
+
+// ------------------------------------------------------------ digit splits
+// Integer digits of x / 2^E truncated to 54 fractional bits, |x| < 2^E.
+__device__ __forceinline__ void digits(double x, int E, uint16_t (&d)[NSL]) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    const int ex = (int)((bits >> 52) & 0x7FF);
+    const unsigned long long man = (bits & ((1ull << 52) - 1)) | (ex ? (1ull << 52) : 0ull);
+    const int sh = (ex ? ex : 1) - 1075 + 54 - E;  // x / 2^E * 2^54 = man * 2^sh, sh <= 1
+    const unsigned long long q = sh >= 0 ? (man << (sh > 1 ? 1 : sh)) : (sh <= -64 ? 0ull : (man >> (-sh)));
+    const uint32_t sgn = (uint32_t)(bits >> 63) << 15;
+#pragma unroll
+    for (int p = 0; p < NSL; ++p) {
+        const uint32_t v = (uint32_t)(q >> (6 * (NSL - 1 - p))) & 63u;
+        const float f = __uint_as_float(0x4B000000u | v) - 8388608.0f;  // exact small integer
+        d[p] = (uint16_t)((__float_as_uint(f) >> 16) | (v ? sgn : 0u));
+    }
+}
+
+__device__ __forceinline__ int exp_above(double m) {  // smallest E with m < 2^E (m >= 0)
+    if (!(m > 0.0)) return 0;
+    int e;
+    frexp(m, &e);
+    return e;
+}
+
+// Rows of X (row-major, ld = K) -> digit tiles.  A warp owns 8 consecutive
+// rows: lane = (octet phase << 3) | row-in-group, so the 8 lanes of one phase
+// store one 128-byte core matrix.  rows_pad = nrt * 128 rows are written
+// (zeros past `rows`).
+__global__ void __launch_bounds__(256) k_oz_split_rows(const double *X, long long rows, int K, int nkc, int nrt,
+                                                       uint8_t *ad, int *rexp) {
+    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31, rr = lane & 7, ph = lane >> 3;
+    const long long row = gw * 8 + rr;
+    if (gw * 8 >= (long long)nrt * BM) return;
+    const bool valid = row < rows;
+    const double *xr = X + (valid ? row : 0) * (long long)K;
+    double mx = 0.0;
+    if (valid)
+        for (int k = ph * 8; k < K; k += 32)
+            for (int e = 0; e < 8 && k + e < K; ++e) mx = fmax(mx, fabs(xr[k + e]));
+    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, 8));
+    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
+    const int E = exp_above(mx);
+    if (ph == 0) rexp[row] = E;
+    const int rt = (int)(row / BM), r = (int)(row % BM);
+    for (int oct = ph; oct < nkc * (KC / 8); oct += 4) {
+        uint32_t w[NSL][4];
+#pragma unroll
+        for (int p = 0; p < NSL; ++p) w[p][0] = w[p][1] = w[p][2] = w[p][3] = 0u;
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            const int k = oct * 8 + e;
+            const double x = (valid && k < K) ? xr[k] : 0.0;
+            uint16_t d[NSL];
+            digits(x, E, d);
+#pragma unroll
+            for (int p = 0; p < NSL; ++p) w[p][e >> 1] |= (uint32_t)d[p] << (16 * (e & 1));
+        }
+        const int kc = oct / (KC / 8), kq = oct % (KC / 8);
+        uint8_t *base = ad + ((size_t)rt * nkc + kc) * A_ROW + kq * LBO_A + (r / 8) * SBO + (r % 8) * 16;
+#pragma unroll
+        for (int p = 0; p < NSL; ++p)
+            *(uint4 *)(base + (size_t)p * A_TILE) = make_uint4(w[p][0], w[p][1], w[p][2], w[p][3]);
+    }
+}
+
+// Columns of A ([K, ncols] row-major, ld = lda) -> digit tiles (one block).
+__global__ void __launch_bounds__(256) k_oz_split_cols(const double *A, int K, int ncols, int lda, int nkc,
+                                                       uint8_t *bd, int *cexp) {
+    __shared__ double smax[256];
+    __shared__ int sE[NB];
+    const int tid = threadIdx.x, c = tid % NB;
+    double mx = 0.0;
+    if (c < ncols)
+        for (int k = tid / NB; k < K; k += 256 / NB) mx = fmax(mx, fabs(A[(long long)k * lda + c]));
+    smax[tid] = mx;
+    __syncthreads();
+    if (tid < NB) {
+        double m = 0.0;
+        for (int i = tid; i < 256; i += NB) m = fmax(m, smax[i]);
+        sE[tid] = exp_above(m);
+        cexp[tid] = sE[tid];
+    }
+    __syncthreads();
+    for (long long i = tid; i < (long long)nkc * KC * NB; i += 256) {
+        const int k = (int)(i / NB), col = (int)(i % NB);
+        const double x = (col < ncols && k < K) ? A[(long long)k * lda + col] : 0.0;
+        uint16_t d[NSL];
+        digits(x, sE[col], d);
+        const int kc = k / KC, kq = (k % KC) / 8, ke = k % 8;
+        for (int q = 0; q < NSL; ++q) {
+            const int row = q * NB + col;
+            *(uint16_t *)(bd + (size_t)kc * B_STAGE + kq * LBO_B + (row / 8) * SBO + (row % 8) * 16 + ke * 2) = d[q];
+        }
+    }
+}
+
+// ------------------------------------------------------------------ host
+size_t OzPlan::bytes() const {
+    const size_t a = (size_t)nrt * nkc * A_ROW, re = (size_t)nrt * BM * sizeof(int);
+    const size_t bb = (size_t)nkc * B_STAGE;
+    return (size_t)njob * (a + re + bb + 256) + 256;
+}
+
+int oz_gemm_skinny(const OzPlan &pl, const double *const *X, const double *const *A, double *const *T, int lda,
+                   int ldt, void *work, cudaStream_t st) {
+    if (pl.njob < 1 || pl.njob > 4 || pl.K < 1 || pl.K > kMaxK || pl.ncols < 1 || pl.ncols > NB) return 1;
+    static bool attr_set = false;
+    if (!attr_set) {
+        if (cudaFuncSetAttribute(k_oz_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) != cudaSuccess)
+            return 2;
+        attr_set = true;
+    }
+    uint8_t *w = (uint8_t *)work;
+    int *err = (int *)w;
+    w += 256;
+    OzBatch b{};
+    b.njob = pl.njob;
+    b.nkc = pl.nkc;
+    b.ncols = pl.ncols;
+    b.ldo = ldt;
+    cudaMemsetAsync(err, 0, sizeof(int), st);
+    for (int j = 0; j < pl.njob; ++j) {
+        uint8_t *ad = w;
+        w += (size_t)pl.nrt * pl.nkc * A_ROW;
+        int *rexp = (int *)w;
+        w += (size_t)pl.nrt * BM * sizeof(int);
+        uint8_t *bd = w;
+        w += (size_t)pl.nkc * B_STAGE;
+        int *cexp = (int *)w;
+        w += 256;
+        const long long warps = (long long)pl.nrt * BM / 8;
+        k_oz_split_rows<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(X[j], pl.rows, pl.K, pl.nkc, pl.nrt, ad,
+                                                                             rexp);
+        k_oz_split_cols<<<1, 256, 0, st>>>(A[j], pl.K, pl.ncols, lda, pl.nkc, bd, cexp);
+        g_launches.fetch_add(2, std::memory_order_relaxed);
+        b.job[j] = OzJob{ad, rexp, bd, cexp, T[j], pl.rows, pl.nrt};
+    }
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long tiles = (long long)pl.njob * pl.nrt;
+    const unsigned grid = (unsigned)(tiles < sms ? tiles : sms);
+    // algorithmic bytes: every digit of X and of A once, the FP64 results once
+    const long long abytes = (long long)pl.njob * ((long long)pl.nrt * pl.nkc * A_ROW + (long long)pl.nkc * B_STAGE +
+                                                   pl.rows * pl.ncols * (long long)sizeof(double));
+    ProfSpan span;
+    span.begin("oz_gemm", st, abytes);
+    k_oz_gemm<<<grid, 192, SMEM_BYTES, st>>>(b, err);
+    span.end();
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    return cudaGetLastError() == cudaSuccess ? 0 : 3;
+}
+
+int oz_check_error(const void *work, cudaStream_t st) {
+    int h = 0;
+    if (cudaMemcpyAsync(&h, work, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) return 3;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return 3;
+    return h ? 4 : 0;
+}
+
+}  // namespace oz
+}  // namespace nvpt

@@ -28,12 +28,14 @@
 // determinant is the ordered product a+_{i1} ... a+_{iN}|0> with ascending
 // spin-orbital indices.  n <= 16 (2n <= 32 bits).
 #include <algorithm>
+#include <numeric>
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
+#include <parallel/algorithm>
 #endif
 
 namespace {
@@ -152,7 +154,13 @@ void gram_block(const Block &blk, I ndet, const uint32_t *amask, const uint32_t 
             else { ++ia[j]; for (int m = j + 1; m < r; ++m) ia[m] = ia[m - 1] + 1; }
         }
     }
+    // keys are unique (one entry per source determinant and annihilation
+    // set), so any sort gives the same order
+#ifdef _OPENMP
+    __gnu_parallel::sort(ent.begin(), ent.end(), [](const Entry &a, const Entry &b) { return a.key < b.key; });
+#else
     std::sort(ent.begin(), ent.end(), [](const Entry &a, const Entry &b) { return a.key < b.key; });
+#endif
     // groups by xid
     const I ne = (I)ent.size();
     std::vector<I> gstart;
@@ -241,26 +249,38 @@ int rdmgen_dense(int n, int k, long ndet, const uint32_t *amask, const uint32_t 
         Block blk{n, k, r, BIN.t[n][r], BIN.t[n][k - r], BIN.t[n][r] * BIN.t[n][k - r]};
         std::vector<double> D((size_t)(blk.dim * blk.dim), 0.0);
         gram_block(blk, ndet, amask, bmask, coef, s, t, D.data());
+        // (rank, sign) of every index tuple under every spin pattern of this block
+        const unsigned nsp = 1u << k;
+        std::vector<int32_t> trk((size_t)nsp * nk, -1);
+        std::vector<int8_t> tsg((size_t)nsp * nk, 0);
+#pragma omp parallel for schedule(static)
+        for (I Q = 0; Q < nk; ++Q) {
+            int qo[4];
+            I y = Q;
+            for (int m = 0; m < k; ++m) { qo[m] = (int)(y % n); y /= n; }
+            for (unsigned sp = 0; sp < nsp; ++sp) {
+                if (k - popc(sp) != r) continue;
+                I Trank;
+                int sg2;
+                if (!spin_tuple_rank(qo, sp, k, r, blk.dimB, &Trank, &sg2)) continue;
+                trk[sp * nk + Q] = (int32_t)Trank;
+                tsg[sp * nk + Q] = (int8_t)sg2;
+            }
+        }
 #pragma omp parallel for schedule(dynamic, 4)
         for (I P = 0; P < nk; ++P) {
-            int po[4], qo[4];
-            I x = P;
-            for (int m = 0; m < k; ++m) { po[m] = (int)(x % n); x /= n; }
-            for (unsigned sp = 0; sp < (1u << k); ++sp) {
-                if (k - popc(sp) != r) continue;
-                I Srank;
-                int sg1;
-                if (!spin_tuple_rank(po, sp, k, r, blk.dimB, &Srank, &sg1)) continue;
-                const double *row = D.data() + Srank * blk.dim;
+            for (unsigned sp = 0; sp < nsp; ++sp) {
+                const int32_t Srank = trk[sp * nk + P];
+                if (Srank < 0) continue;
+                const int sg1 = tsg[sp * nk + P];
+                const double *row = D.data() + (I)Srank * blk.dim;
+                const int32_t *tr = trk.data() + sp * nk;
+                const int8_t *ts = tsg.data() + sp * nk;
                 for (I Q = 0; Q < nk; ++Q) {
-                    I y = Q;
-                    for (int m = 0; m < k; ++m) { qo[m] = (int)(y % n); y /= n; }
-                    I Trank;
-                    int sg2;
-                    if (!spin_tuple_rank(qo, sp, k, r, blk.dimB, &Trank, &sg2)) continue;
-                    double v = row[Trank];
+                    if (tr[Q] < 0) continue;
+                    double v = row[tr[Q]];
                     if (v == 0.0) continue;
-                    out[slot + ldo * (P + nk * Q)] += (sg1 * sg2) * v;
+                    out[slot + ldo * (P + nk * Q)] += (sg1 * ts[Q]) * v;
                 }
             }
         }
@@ -293,31 +313,53 @@ int rdmgen_ro4(int n, long ndet, const uint32_t *amask, const uint32_t *bmask, c
         for (int m = 0; m < 4; ++m) { q[m] = (int)(y % n) + 1; y /= n; }
         nm[L] = normind(q[0], q[1], q[2], q[3]);
     }
+    // L in ascending normind order; the slots of key `ind` are the first
+    // upto[ind] of them
+    std::vector<I> lord(n4);
+    std::iota(lord.begin(), lord.end(), (I)0);
+    std::stable_sort(lord.begin(), lord.end(), [&](I a, I b) { return nm[a] < nm[b]; });
+    std::vector<I> upto(W + 1, 0);
+    for (I L = 0; L < n4; ++L) upto[nm[L]]++;
+    for (I v = 1; v <= W; ++v) upto[v] += upto[v - 1];
+    std::vector<int32_t> trk((size_t)16 * n4);
+    std::vector<int8_t> tsg((size_t)16 * n4);
     for (int r = 0; r <= k; ++r) {
         Block blk{n, k, r, BIN.t[n][r], BIN.t[n][k - r], BIN.t[n][r] * BIN.t[n][k - r]};
         std::vector<double> D((size_t)(blk.dim * blk.dim), 0.0);
         gram_block(blk, ndet, amask, bmask, coef, s, s, D.data());
+        // (rank, sign) of every L under every spin pattern of this block
+#pragma omp parallel for schedule(static)
+        for (I L = 0; L < n4; ++L) {
+            I y = L;
+            int q[4];
+            for (int m = 0; m < 4; ++m) { q[m] = (int)(y % n); y /= n; }
+            for (unsigned sp = 0; sp < 16u; ++sp) {
+                I Trank;
+                int sg2;
+                const bool ok = (k - popc(sp) == r) && spin_tuple_rank(q, sp, k, r, blk.dimB, &Trank, &sg2);
+                trk[sp * n4 + L] = ok ? (int32_t)Trank : -1;
+                tsg[sp * n4 + L] = ok ? (int8_t)sg2 : 0;
+            }
+        }
 #pragma omp parallel for schedule(dynamic, 8)
         for (I kk = 0; kk < nkeys; ++kk) {
             int K[4] = {keys[4 * kk] - 1, keys[4 * kk + 1] - 1, keys[4 * kk + 2] - 1, keys[4 * kk + 3] - 1};
             I ind = lind(K[0] + 1, K[1] + 1, K[2] + 1, K[3] + 1);
+            const I lim = upto[ind];
             for (unsigned sp = 0; sp < 16u; ++sp) {
                 if (k - popc(sp) != r) continue;
                 I Srank;
                 int sg1;
                 if (!spin_tuple_rank(K, sp, k, r, blk.dimB, &Srank, &sg1)) continue;
                 const double *row = D.data() + Srank * blk.dim;
-                for (I L = 0; L < n4; ++L) {
-                    if (nm[L] > ind) continue;
-                    I y = L;
-                    int q[4];
-                    for (int m = 0; m < 4; ++m) { q[m] = (int)(y % n); y /= n; }
-                    I Trank;
-                    int sg2;
-                    if (!spin_tuple_rank(q, sp, k, r, blk.dimB, &Trank, &sg2)) continue;
-                    double v = row[Trank];
+                const int32_t *tr = trk.data() + sp * n4;
+                const int8_t *ts = tsg.data() + sp * n4;
+                for (I i = 0; i < lim; ++i) {
+                    const I L = lord[i];
+                    if (tr[L] < 0) continue;
+                    double v = row[tr[L]];
                     if (v == 0.0) continue;
-                    ro4_s[(ind - 1) + W * L] += (sg1 * sg2) * v;
+                    ro4_s[(ind - 1) + W * L] += (sg1 * ts[L]) * v;
                 }
             }
         }

@@ -22,6 +22,27 @@ def context() -> Context:
     return _ctx
 
 
+FP64, SPLIT = 0, 1
+
+
+class precision:
+    """Context manager selecting the contraction precision of the shared
+    context (nvpt_set_precision): ``with koopro.precision(koopro.SPLIT): ...``."""
+
+    def __init__(self, mode: int, ctx: Context | None = None):
+        self.mode, self.ctx = mode, ctx
+
+    def __enter__(self):
+        c = self.ctx or context()
+        self.prev = int(c._lib.nvpt_get_precision(c.handle))
+        c.call("nvpt_set_precision", self.mode)
+        return c
+
+    def __exit__(self, *exc):
+        (self.ctx or context()).call("nvpt_set_precision", self.prev)
+        return False
+
+
 def _f(a) -> np.ndarray:
     a = np.asarray(a, dtype=np.float64)
     return a if a.flags.f_contiguous else np.asfortranarray(a)
