@@ -59,6 +59,9 @@ int64_t nvpt_nwords(int64_t nact);
  * (1-based, row of 8 per tuple); out8 receives (i1..i8) per tuple and
  * lindex receives lindice(i1,i2,i3,i4) (src/indices_norm.F90:64). */
 int nvpt_ord8(nvpt_context *ctx, int64_t nact, int64_t count, const int64_t *in8, int64_t *out8, int64_t *lindex);
+/* src/ord_utils.F90:16 ord9 (same arguments as nvpt_ord8): exchange-sort
+ * variant, not called on the Koopmans/NEVPT2 path, kept bit-exact. */
+int nvpt_ord9(nvpt_context *ctx, int64_t nact, int64_t count, const int64_t *in8, int64_t *out8, int64_t *lindex);
 
 /* ------------------------------------------------------------------ */
 /* Stage 1 (koopro4QD.x): RDM partial traces, integrals, Koopmans.     */
@@ -137,14 +140,34 @@ int nvpt_bdmat_d(nvpt_context *ctx, const double *atwo, double *dmat, double *dt
                  const double *dal, int64_t nact, int64_t ncore, double *f, const double *aj, int64_t metat,
                  void *stream);
 
+/* src/rdm_utils.F90:236 permute_4rdm / :470 permute_3rdm as applied by
+ * hdf5_read_rdm_from_resfile (:193-226) to a QCMaquis label/value list:
+ * labels are the file's 0-based int32 indices, label-major (8 per entry for
+ * the 4-RDM, 6 for the 3-RDM), values the entries in file order.  Every
+ * entry writes its images (assignments; a later entry overwrites an earlier
+ * one) into ro4(W,n,n,n,n) of one state, or into the 3-RDM element
+ * (i,j,k,l,m,n) at rdm3[ld*((i-1)+n((j-1)+...))] (ld = metat for daaa(s,...)
+ * with rdm3 pointing at the state's first element).  trans != 0: transition
+ * 3-RDM (6 images, value not negated).  Elements no entry writes keep their
+ * values.  A label outside [0,nact) returns NVPT_EINVAL. */
+int nvpt_permute_4rdm(nvpt_context *ctx, double *ro4, int64_t nact, const int32_t *labels, const double *values,
+                      int64_t nentries);
+int nvpt_permute_3rdm(nvpt_context *ctx, double *rdm3, int64_t ld, int64_t nact, const int32_t *labels,
+                      const double *values, int64_t nentries, int trans);
+int nvpt_permute_4rdm_d(nvpt_context *ctx, double *ro4, int64_t nact, const int32_t *labels, const double *values,
+                        int64_t nentries, void *stream);
+int nvpt_permute_3rdm_d(nvpt_context *ctx, double *rdm3, int64_t ld, int64_t nact, const int32_t *labels,
+                        const double *values, int64_t nentries, int trans, void *stream);
+
 /* Precision of the dense contractions of later calls on ctx (no counterpart
  * in the reference).  NVPT_PRECISION_FP64 (the default) is the drop-in.
  * NVPT_PRECISION_SPLIT runs the n^9 slab products of bamat as Ozaki digit
  * products on the tensor cores: each FP64 operand row/column is scaled by a
- * power of two and cut into nine 6-bit digits held exactly in BF16, every
- * digit pair with weight >= 2^-60 is summed exactly in FP32, and the partial
- * products are recombined in FP64 (error below 2^-51 of the row/column
- * maximum per product).  Eigensolves, pseudo-inverses, denominators and
+ * power of two, rounded to 60 bits and cut into ten 6-bit digits held
+ * exactly in BF16, every digit pair with weight >= 2^-72 is summed exactly in
+ * FP32, and the partial products are recombined in FP64 (error about 2^-61
+ * of the row/column maximum per product).  Eigensolves, pseudo-inverses,
+ * denominators and
  * energy sums always run in FP64. */
 #define NVPT_PRECISION_FP64 0
 #define NVPT_PRECISION_SPLIT 1

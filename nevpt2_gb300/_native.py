@@ -55,6 +55,7 @@ _SIGS = {
     "nvpt_launch_count": ([P], I64),
     "nvpt_nwords": ([I64], I64),
     "nvpt_ord8": ([P, I64, I64, P, P, P], ctypes.c_int),
+    "nvpt_ord9": ([P, I64, I64, P, P, P], ctypes.c_int),
     "nvpt_bro3": ([P, P, P, I64, I64, I64], ctypes.c_int),
     "nvpt_bro2": ([P, P, P, I64, I64, I64], ctypes.c_int),
     "nvpt_bro1": ([P, P, P, I64, I64, I64], ctypes.c_int),
@@ -71,6 +72,10 @@ _SIGS = {
     "nvpt_koop_matrices_ctl_d": ([P, I64, I64, I64] + [P] * 14 + [P], ctypes.c_int),
     "nvpt_bamat_d": ([P] + [P] * 7 + [I64, I64, P, P, I64, I64, I64, P], ctypes.c_int),
     "nvpt_bamat_static_d": ([P] + [P] * 7 + [I64, I64, P, P, I64, I64, I64, P], ctypes.c_int),
+    "nvpt_permute_4rdm": ([P, P, I64, P, P, I64], ctypes.c_int),
+    "nvpt_permute_3rdm": ([P, P, I64, I64, P, P, I64, ctypes.c_int], ctypes.c_int),
+    "nvpt_permute_4rdm_d": ([P, P, I64, P, P, I64, P], ctypes.c_int),
+    "nvpt_permute_3rdm_d": ([P, P, I64, I64, P, P, I64, ctypes.c_int, P], ctypes.c_int),
     "nvpt_set_precision": ([P, ctypes.c_int], ctypes.c_int),
     "nvpt_get_precision": ([P], ctypes.c_int),
     "nvpt_dgemm_split_d": ([P, I64, I64, I64, P, P, P, P], ctypes.c_int),

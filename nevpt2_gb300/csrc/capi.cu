@@ -70,6 +70,18 @@ __global__ void k_ord8(const int64_t *in8, int64_t *out8, int64_t *lindex, long 
     lindex[t] = ind;
 }
 
+// src/ord_utils.F90:16 ord9 over a batch of tuples.
+__global__ void k_ord9(const int64_t *in8, int64_t *out8, int64_t *lindex, long long count) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const int64_t *x = in8 + 8 * t;
+    int o[8];
+    int ind = ord9_key((int)x[0], (int)x[1], (int)x[2], (int)x[3], (int)x[4], (int)x[5], (int)x[6], (int)x[7], o[0],
+                       o[1], o[2], o[3], o[4], o[5], o[6], o[7]);
+    for (int i = 0; i < 8; ++i) out8[8 * t + i] = o[i];
+    lindex[t] = ind;
+}
+
 void launch_ord8(const int64_t *in8, int64_t *out8, int64_t *lindex, long long count, cudaStream_t st) {
     k_ord8<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(in8, out8, lindex, count);
     g_launches.fetch_add(1, std::memory_order_relaxed);
@@ -161,6 +173,16 @@ struct Stage {
         if (e != cudaSuccess) { status = cuda_check(ctx, e, "H2D copy"); return nullptr; }
         return d;
     }
+    void *up_bytes(const void *h, size_t bytes) {
+        if (status != NVPT_OK) return nullptr;
+        void *p = nullptr;
+        cudaError_t e = cudaMallocAsync(&p, bytes > 0 ? bytes : 1, st);
+        if (e != cudaSuccess) { status = cuda_check(ctx, e, "cudaMallocAsync"); return nullptr; }
+        bufs.push_back(p);
+        e = cudaMemcpyAsync(p, h, bytes, cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) { status = cuda_check(ctx, e, "H2D copy"); return nullptr; }
+        return p;
+    }
     int down(double *h, const double *d, int64_t count) {
         if (status != NVPT_OK) return status;
         cudaError_t e = cudaMemcpyAsync(h, d, sizeof(double) * (size_t)count, cudaMemcpyDeviceToHost, st);
@@ -251,6 +273,27 @@ int nvpt_ord8(nvpt_context *ctx, int64_t nact, int64_t count, const int64_t *in8
     cudaMemcpyAsync(lindex, d + 16 * count, sizeof(int64_t) * count, cudaMemcpyDeviceToHost, st);
     cudaFreeAsync(d, st);
     int rc2 = cuda_check(ctx, cudaStreamSynchronize(st), "ord8 sync");
+    return rc != NVPT_OK ? rc : rc2;
+}
+
+int nvpt_ord9(nvpt_context *ctx, int64_t nact, int64_t count, const int64_t *in8, int64_t *out8, int64_t *lindex) {
+    NV_TRY(check_nact(ctx, nact, 1));
+    if (count < 0 || (count > 0 && (!in8 || !out8 || !lindex))) return fail(ctx, NVPT_EINVAL, "ord9: bad buffers");
+    for (int64_t i = 0; i < 8 * count; ++i)
+        if (in8[i] < 1 || in8[i] > nact) return fail(ctx, NVPT_EINVAL, "ord9: index outside [1,nact]");
+    if (count == 0) return NVPT_OK;
+    cudaStream_t st = ctx->stream;
+    int64_t *d = nullptr;
+    size_t bytes = sizeof(int64_t) * (size_t)count * 17;
+    NV_TRY(cuda_check(ctx, cudaMallocAsync((void **)&d, bytes, st), "cudaMallocAsync"));
+    cudaMemcpyAsync(d, in8, sizeof(int64_t) * 8 * count, cudaMemcpyHostToDevice, st);
+    k_ord9<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(d, d + 8 * count, d + 16 * count, count);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    int rc = after_launch(ctx, "ord9 launch");
+    cudaMemcpyAsync(out8, d + 8 * count, sizeof(int64_t) * 8 * count, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(lindex, d + 16 * count, sizeof(int64_t) * count, cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(d, st);
+    int rc2 = cuda_check(ctx, cudaStreamSynchronize(st), "ord9 sync");
     return rc != NVPT_OK ? rc : rc2;
 }
 
@@ -352,6 +395,49 @@ int nvpt_bamat_static_d(nvpt_context *ctx, double *amat, double *atmat, const do
     launch_build_f(f, aj, atwo, (int)nact, (int)ncore, 1, st);
     launch_bamat_static(r, atwo, f, (int)ncore, amat, atmat, st, scr);
     return after_launch(ctx, "bamat_static");
+}
+
+// Device part of the label/value unfolding: scratch, the two passes, the
+// label check.
+static int unfold_d(nvpt_context *ctx, int which, double *dst, int64_t ld, int64_t nact, const int32_t *labels,
+                    const double *values, int64_t nentries, int trans, cudaStream_t st) {
+    NV_TRY(check_nact(ctx, nact, 1));
+    if (nentries < 0 || !dst || (nentries > 0 && (!labels || !values)) || ld < 1)
+        return fail(ctx, NVPT_EINVAL, "permute_rdm: bad arguments");
+    const int64_t n = nact, W = n * (n + 1) * (n + 2) * (n + 3) / 24;
+    const int64_t slots = which == 4 ? W * n * n * n * n : n * n * n * n * n * n;
+    unsigned long long *owner = nullptr;
+    int *bad = nullptr;
+    NV_TRY(cuda_check(ctx, cudaMallocAsync((void **)&owner, sizeof(unsigned long long) * slots, st), "permute_rdm"));
+    if (cudaMallocAsync((void **)&bad, sizeof(int), st) != cudaSuccess) {
+        cudaFreeAsync(owner, st);
+        return fail(ctx, NVPT_ENOMEM, "permute_rdm: device allocation failed");
+    }
+    cudaMemsetAsync(bad, 0, sizeof(int), st);
+    int rc = which == 4 ? launch_unfold4(labels, values, nentries, (int)n, dst, owner, bad, st)
+                        : launch_unfold3(labels, values, nentries, (int)n, dst, ld, trans != 0, owner, bad, st);
+    int hbad = 0;
+    if (!rc) {
+        cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st);
+        if (cudaStreamSynchronize(st) != cudaSuccess) rc = 1;
+    }
+    cudaFreeAsync(bad, st);
+    cudaFreeAsync(owner, st);
+    if (rc) return cuda_check(ctx, cudaGetLastError(), "permute_rdm");
+    if (hbad) return fail(ctx, NVPT_EINVAL, "permute_rdm: a label index is outside [0, nact)");
+    return after_launch(ctx, "permute_rdm");
+}
+
+int nvpt_permute_4rdm_d(nvpt_context *ctx, double *ro4, int64_t nact, const int32_t *labels, const double *values,
+                        int64_t nentries, void *stream) {
+    if (!ctx) return NVPT_EINVAL;
+    return unfold_d(ctx, 4, ro4, 1, nact, labels, values, nentries, 0, pick(ctx, stream));
+}
+
+int nvpt_permute_3rdm_d(nvpt_context *ctx, double *rdm3, int64_t ld, int64_t nact, const int32_t *labels,
+                        const double *values, int64_t nentries, int trans, void *stream) {
+    if (!ctx) return NVPT_EINVAL;
+    return unfold_d(ctx, 3, rdm3, ld, nact, labels, values, nentries, trans, pick(ctx, stream));
 }
 
 int nvpt_set_precision(nvpt_context *ctx, int precision) {
@@ -545,6 +631,33 @@ int nvpt_bamat(nvpt_context *ctx, double *amat, double *atmat, const double *atw
     NV_TRY(nvpt_bamat_d(ctx, o_a, o_at, d_atwo, d_ro4, d3, d2, d1, nact, ncore, d_f, d_aj, norb, metat, nsym, nullptr));
     S.down(amat, o_a, n6 * M); S.down(atmat, o_at, n6 * M); S.down(f, d_f, nf);
     return S.finish();
+}
+
+static int unfold_host(nvpt_context *ctx, int which, double *dst, int64_t ld, int64_t nact, const int32_t *labels,
+                       const double *values, int64_t nentries, int trans) {
+    NV_TRY(check_nact(ctx, nact, 1));
+    if (nentries < 0 || ld < 1) return fail(ctx, NVPT_EINVAL, "permute_rdm: bad arguments");
+    const int64_t n = nact, W = nvpt_nwords(nact);
+    const int64_t count = which == 4 ? W * ipow(n, 4) : ld * ipow(n, 6);
+    Stage S(ctx);
+    double *d = S.up(dst, count);
+    const int32_t *l = nentries ? (const int32_t *)S.up_bytes(labels, sizeof(int32_t) * (which == 4 ? 8 : 6) * nentries)
+                                : nullptr;
+    const double *v = nentries ? S.up(values, nentries) : nullptr;
+    if (S.status) return S.status;
+    NV_TRY(unfold_d(ctx, which, d, ld, nact, l, v, nentries, trans, ctx->stream));
+    S.down(dst, d, count);
+    return S.finish();
+}
+
+int nvpt_permute_4rdm(nvpt_context *ctx, double *ro4, int64_t nact, const int32_t *labels, const double *values,
+                      int64_t nentries) {
+    return unfold_host(ctx, 4, ro4, 1, nact, labels, values, nentries, 0);
+}
+
+int nvpt_permute_3rdm(nvpt_context *ctx, double *rdm3, int64_t ld, int64_t nact, const int32_t *labels,
+                      const double *values, int64_t nentries, int trans) {
+    return unfold_host(ctx, 3, rdm3, ld, nact, labels, values, nentries, trans);
 }
 
 static int bcd_host(nvpt_context *ctx, int which, const double *atwo, double *x, double *xt, const double *daaa,

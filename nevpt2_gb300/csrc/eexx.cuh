@@ -57,6 +57,34 @@ __host__ __device__ __forceinline__ int ord8_key(int a1, int c1, int e1, int g1,
     return lindice4(k[0], k[1], k[2], k[3]);
 }
 
+// ord9 of src/ord_utils.F90:16-68: the same key choice as ord8, but the key
+// is exchange-sorted (every larger later element is swapped into place at
+// once, and the partner swapped with it), which differs from ord8 on ties.
+// Returns lindice of the sorted key; k0..k3 the key, p0..p3 the partner.
+__host__ __device__ __forceinline__ int ord9_key(int a1, int c1, int e1, int g1, int a2, int c2, int e2, int g2,
+                                                 int &k0, int &k1, int &k2, int &k3, int &p0, int &p1, int &p2,
+                                                 int &p3) {
+    int k[4], p[4];
+    if (normind4(a1, c1, e1, g1) >= normind4(a2, c2, e2, g2)) {
+        k[0] = a1; k[1] = c1; k[2] = e1; k[3] = g1;
+        p[0] = a2; p[1] = c2; p[2] = e2; p[3] = g2;
+    } else {
+        k[0] = a2; k[1] = c2; k[2] = e2; k[3] = g2;
+        p[0] = a1; p[1] = c1; p[2] = e1; p[3] = g1;
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = i + 1; j < 4; ++j)
+            if (k[j] > k[i]) {
+                int t = k[i]; k[i] = k[j]; k[j] = t;
+                t = p[i]; p[i] = p[j]; p[j] = t;
+            }
+    k0 = k[0]; k1 = k[1]; k2 = k[2]; k3 = k[3];
+    p0 = p[0]; p1 = p[1]; p2 = p[2]; p3 = p[3];
+    return lindice4(k[0], k[1], k[2], k[3]);
+}
+
 // Views of the spin-free RDMs of one problem, reference layouts.
 struct Rdm {
     int n, M;

@@ -58,6 +58,12 @@ struct ProfSpan {
     void begin(const char *t, cudaStream_t s, long long nbytes);
     void end();
 };
+// QCMaquis label/value unfolding (rdm_unfold.cu); owner: one word per
+// destination element; *bad set if a label is out of range.  0 on success.
+int launch_unfold4(const int32_t *labels, const double *values, long long nentries, int n, double *ro4,
+                   unsigned long long *owner, int *bad, cudaStream_t st);
+int launch_unfold3(const int32_t *labels, const double *values, long long nentries, int n, double *rdm3,
+                   long long ld, bool trans, unsigned long long *owner, int *bad, cudaStream_t st);
 void launch_ord8(const int64_t *in8, int64_t *out8, int64_t *lindex, long long count, cudaStream_t st);
 
 }  // namespace nvpt

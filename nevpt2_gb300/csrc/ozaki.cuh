@@ -9,23 +9,32 @@ namespace nvpt {
 namespace oz {
 
 constexpr int BM = 128;                // rows per tile (UMMA M)
-constexpr int KC = 32;                 // K columns per pipeline stage
-constexpr int NSL = 9;                 // 6-bit digit slices per operand (54 bits)
+constexpr int KC = 64;                 // K columns per pipeline stage: one 128-byte swizzle atom per row
+constexpr int NSL = 10;                // 6-bit digit slices per operand (60 bits)
 constexpr int NB = 16;                 // output columns (padded) per slice
 constexpr int NBT = NSL * NB;          // B rows per stage (all q-slices)
-constexpr int A_TILE = BM * KC * 2;    // bytes of one slice of one stage
-constexpr int B_STAGE = NBT * KC * 2;  // 9216
-// The digit pairs (p, q), p + q <= NSL - 1, need 720 TMEM columns; they run
-// in two passes over K, p in [0,4) (480 columns) and p in [4,9) (240).
-constexpr int NPASS = 2;
-constexpr int PASS_SPLIT = 4;  // first slice of the second pass
-__host__ __device__ constexpr int pass_p0(int pass) { return pass == 0 ? 0 : pass == 1 ? PASS_SPLIT : NSL; }
-constexpr int MAX_PASS_SLICES = 5;
-constexpr int A_STAGE = MAX_PASS_SLICES * A_TILE;  // 40960
-constexpr int STAGES = 4;
-constexpr int LBO_A = BM * 16;   // next 8-column K octet
-constexpr int LBO_B = NBT * 16;
-constexpr int SBO = 128;         // next 8-row group
+constexpr int ROWB = KC * 2;           // bytes of one row of a stage (128)
+constexpr int A_TILE = BM * ROWB;      // bytes of one slice of one stage (16 KB)
+constexpr int B_STAGE = NBT * ROWB;    // 20 KB
+// Digit pairs kept: p + q <= TMAX (p, q < NSL), 64 pairs = 1024 TMEM columns
+// of 16.  They run in NPASS passes over K, groups of consecutive slices p
+// whose pairs fit TMEM (512 columns).  nq(p) = number of q-slices paired
+// with p; one MMA per slice p and K step covers all its q-slices.
+constexpr int TMAX = 10;
+__host__ __device__ constexpr int nq(int p) { return (TMAX - p + 1) < NSL ? (TMAX - p + 1) : NSL; }
+constexpr int NPASS = 4;
+__host__ __device__ constexpr int pass_p0(int pass) {  // slices {0,1,2}, {3,4,5}, {6,7}, {8,9}
+    return pass == 0 ? 0 : pass == 1 ? 3 : pass == 2 ? 6 : pass == 3 ? 8 : NSL;
+}
+constexpr int MAX_PASS_SLICES = 3;
+constexpr int A_STAGE = MAX_PASS_SLICES * A_TILE;  // 48 KB
+constexpr int STAGES = 3;
+constexpr int EPI_WARPS = 8;           // two per TMEM lane quadrant, 8 output columns each
+constexpr int THREADS = 32 * (EPI_WARPS + 2);
+// Operand tiles in shared memory (and in HBM) are K-major with the 128-byte
+// swizzle: row r of a tile occupies bytes [128 r, 128 r + 128), its 16-byte
+// chunk c stored at chunk c ^ (r mod 8); 8-row groups are 1024 bytes apart.
+constexpr int SBO_SW = 1024;
 constexpr int TMEM_COLS = 512;
 constexpr int SMEM_BYTES = STAGES * (A_STAGE + B_STAGE) + 1024;  // + 1 KB for aligning the base
 constexpr int kMaxK = 4096;      // exact FP32 digit sums need 63*63*K < 2^24

@@ -17,6 +17,7 @@
 #include <functional>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <thread>
 #include <exception>
 #include <vector>
@@ -214,8 +215,27 @@ struct PcResult {
 };
 
 // src/qdnevpt.F:1963-2033 and siblings: the PC metric sequence.
+// Metrics of at least this order take the generalised-eigenproblem route
+// when every metric eigenvalue is above the threshold.
+constexpr long long kPcCholMin = 512;
+
 PcResult pc_transform(Ctx &c, const T &S, const T &K, long long nd, double thr) {
     PcResult r;
+    if (nd >= kPcCholMin && metric_above(c, S.p, nd, thr)) {
+        // Every eigenvalue of S is kept (nnew = nd), so the orthonormalised
+        // Koopmans eigenproblem X^T K X y = w y, X = U w_S^-1/2, is the pencil
+        // K v = w S v with v = X y: same eigenvalues and, up to rotations
+        // inside degenerate eigenspaces, the same PC coefficients C = X Y.
+        // One Cholesky-based solve replaces the metric eigensolve and the
+        // three order-nd GEMMs around it.
+        T w = alloc(c, {nd}, false), V = alloc(c, {nd, nd}, false);
+        if (sygvd_upper(c, K.p, S.p, nd, w.p, V.p)) {
+            r.nnew = (int)nd;
+            r.w = std::move(w);
+            r.C = permuted(c, V, {1, 0});  // C[i][mu] = V[mu][i]
+            return r;
+        }
+    }
     T w = alloc(c, {nd}, false), V = alloc(c, {nd, nd}, false);
     eigh_upper(c, S.p, nd, w.p, V.p);
     std::vector<double> wh(nd);
@@ -1264,7 +1284,7 @@ class Runner {
             build_eee2L(c, P->d3.p, P->d2.p, P->d1.p, n, E3o.p);
             T ro = alloc(c, {n, n}, false), W2o = alloc(c, {n, n, n, n}, false);
             T W3o = alloc(c, {n, n, n, n, n, n}, false);
-            const T *e2src = &E2o, *e3src = &E3o;
+            const T *e3src = &E3o;
             T E2a, E2b, E3t;
             if (minus) {
                 // h daoff(a,ap) h (j<i) / daoff(ap,a): [ap,a]
@@ -1284,7 +1304,6 @@ class Runner {
                 build_eee2tL(c, E3o.p, E2o.p, n, E3t.p);
                 e3src = &E3t;
             }
-            (void)e2src;
             // j<i: (cp,ap,bp,b,a,c); j>i: (c,a,b,bp,ap,cp) at [ap,bp,cp,a,b,c]
             if (lt) permute(c, e3src->p, {n, n, n, n, n, n}, {1, 2, 0, 4, 3, 5}, W3o.p);
             else permute(c, e3src->p, {n, n, n, n, n, n}, {4, 3, 5, 1, 2, 0}, W3o.p);
@@ -1302,16 +1321,18 @@ class Runner {
         K = view2(std::move(K), n3, n3);
         PcResult P = pc_transform(c, S, K, n3, thr);
         acc.nnew[(minus ? 7 : 6) + 10 * s] = P.nnew;
-        T sm = matmul(c, S, false, P.C, false);              // s[(abc), mu]
         T W2t = permuted(c, W2, {3, 0, 1, 2});                 // [a, (ap,bp,cp)]
         W2t = view2(std::move(W2t), n, n3);
-        T spm = matmul(c, W2t, false, P.C, false);            // [a, mu]
-        auto rm = [&](const T &s_, const T &sp_, double *out) {
-            gemm(c, false, false, L, n3, n, 1.0, H.p, n, sp_.p, n3, 0.0, out, n3);
-            gemm(c, false, false, L, n3, n3, 1.0, Vd.p, n3, s_.p, n3, 1.0, out, n3);
+        // R[l, mu] = sum_x (Vd S + H W2t)[l, x] C[x, mu]: the order-n3 products
+        // S C and W2t C of the reference are reassociated onto the L rows.
+        auto rm = [&](const T &S_, const T &W2_, double *out) {
+            T Z = alloc(c, {L, (long long)n3}, false);
+            gemm(c, false, false, L, n3, n3, 1.0, Vd.p, n3, S_.p, n3, 0.0, Z.p, n3);
+            gemm(c, false, false, L, n3, n, 1.0, H.p, n, W2_.p, n3, 1.0, Z.p, n3);
+            gemm(c, false, false, L, n3, n3, 1.0, Z.p, n3, P.C.p, n3, 0.0, out, n3);
         };
         T R = alloc(c, {L, (long long)n3}, false);
-        rm(sm, spm, R.p);
+        rm(S, W2t, R.p);
         T Rj = stack_others(L, n3, [&](int j, double *out) {
             auto [PD, lt] = off(j);
             T E2o = alloc(c, {n, n, n, n}, false), E3o = alloc(c, {n, n, n, n, n, n}, false);
@@ -1344,11 +1365,9 @@ class Runner {
             }
             T So = permuted(c, W3o, {3, 4, 5, 0, 1, 2});
             So = view2(std::move(So), n3, n3);
-            T smj = matmul(c, So, false, P.C, false);
             T W2ot = permuted(c, W2o, {3, 0, 1, 2});
             W2ot = view2(std::move(W2ot), n, n3);
-            T spj = matmul(c, W2ot, false, P.C, false);
-            rm(smj, spj, out);
+            rm(So, W2ot, out);
         });
         std::vector<double> pb(L);  // deno = w + eps_r  /  w - eps_i
         for (long long l = 0; l < L; ++l) pb[l] = -base[l];
@@ -1392,32 +1411,66 @@ T fortran_slice(Ctx &c, const T &F, long long P, long long slot, int n, int k) {
     return out;
 }
 
-// One non-blocking stream with its own cuBLAS/cuSOLVER handles per class,
-// plus the events that order them against the caller's stream.
+// Non-blocking streams, each with its own cuBLAS/cuSOLVER handles, kept for
+// the life of the process (one pool per device) and lent to the concurrent
+// state / class tasks of a call; events order them against the caller's
+// stream.
+class CtxPool {
+  public:
+    static std::vector<Ctx> acquire(size_t n, int dev) {
+        CtxPool &p = get();
+        std::lock_guard<std::mutex> g(p.mu_);
+        std::vector<Ctx> out;
+        auto &free = p.free_[dev];
+        while (out.size() < n && !free.empty()) {
+            out.push_back(free.back());
+            free.pop_back();
+        }
+        while (out.size() < n) {
+            Ctx c{nullptr, nullptr, nullptr};
+            ck(cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking), "cudaStreamCreate");
+            ck(cublasCreate(&c.blas), "cublasCreate");
+            ck(cublasSetStream(c.blas, c.st), "cublasSetStream");
+            ck(cusolverDnCreate(&c.sol), "cusolverDnCreate");
+            ck(cusolverDnSetStream(c.sol, c.st), "cusolverDnSetStream");
+            out.push_back(c);
+        }
+        return out;
+    }
+    static void release(std::vector<Ctx> &v, int dev) {
+        CtxPool &p = get();
+        std::lock_guard<std::mutex> g(p.mu_);
+        for (auto &c : v) p.free_[dev].push_back(c);
+        v.clear();
+    }
+
+  private:
+    static CtxPool &get() {
+        static CtxPool pool;
+        return pool;
+    }
+    std::mutex mu_;
+    std::map<int, std::vector<Ctx>> free_;
+};
+
 struct ClassStreams {
+    int dev = 0;
     std::vector<Ctx> c;
     std::vector<cudaEvent_t> done;
     cudaEvent_t prep = nullptr;
-    explicit ClassStreams(size_t n) : c(n, Ctx{nullptr, nullptr, nullptr}), done(n, nullptr) {
+    explicit ClassStreams(size_t n) : done(n, nullptr) {
+        ck(cudaGetDevice(&dev), "cudaGetDevice");
+        c = CtxPool::acquire(n, dev);
         ck(cudaEventCreateWithFlags(&prep, cudaEventDisableTiming), "cudaEventCreate");
-        for (size_t k = 0; k < n; ++k) {
-            ck(cudaStreamCreateWithFlags(&c[k].st, cudaStreamNonBlocking), "cudaStreamCreate");
-            ck(cudaEventCreateWithFlags(&done[k], cudaEventDisableTiming), "cudaEventCreate");
-            ck(cublasCreate(&c[k].blas), "cublasCreate");
-            ck(cublasSetStream(c[k].blas, c[k].st), "cublasSetStream");
-            ck(cusolverDnCreate(&c[k].sol), "cusolverDnCreate");
-            ck(cusolverDnSetStream(c[k].sol, c[k].st), "cusolverDnSetStream");
-        }
+        for (size_t k = 0; k < n; ++k) ck(cudaEventCreateWithFlags(&done[k], cudaEventDisableTiming), "cudaEventCreate");
     }
     ~ClassStreams() {
         for (size_t k = 0; k < c.size(); ++k) {
-            if (c[k].st) cudaStreamSynchronize(c[k].st);
-            if (c[k].blas) cublasDestroy(c[k].blas);
-            if (c[k].sol) cusolverDnDestroy(c[k].sol);
+            cudaStreamSynchronize(c[k].st);
             if (done[k]) cudaEventDestroy(done[k]);
-            if (c[k].st) cudaStreamDestroy(c[k].st);
         }
         if (prep) cudaEventDestroy(prep);
+        CtxPool::release(c, dev);
     }
 };
 
@@ -1533,35 +1586,66 @@ int run_qdnevpt(nvpt_context *ctx, cudaStream_t st, const nvpt_qdnevpt_in *in, n
     if (m & 64u) jobs.push_back([pc](Runner &r) { r.class_pm1p(true, pc); });
     if (m & 32u) jobs.push_back([pc](Runner &r) { r.class_pm1p(false, pc); });
     const size_t nj = jobs.size();
-    ClassStreams cs(nj);
-    for (int s = 0; s < M; ++s) {
-        R.prepare_state(s);
-        for (int k = 0; k < norb; ++k) epsnew[k + (size_t)norb * s] = R.eps[k];
-        ck(cudaEventRecord(cs.prep, c.st), "event");
-        std::vector<Accum> local(nj, Accum(M));
-        std::vector<std::exception_ptr> fail(nj);
-        int dev = 0;
-        ck(cudaGetDevice(&dev), "cudaGetDevice");
-        auto work = [&](size_t k) {
+    // The states are independent too: every state is prepared on its own
+    // stream, then every (state, class) pair runs concurrently.  The
+    // accumulators are merged state by state in the reference's class order.
+    int dev = 0;
+    ck(cudaGetDevice(&dev), "cudaGetDevice");
+    ClassStreams ps((size_t)M), cs((size_t)M * nj);
+    ck(cudaEventRecord(ps.prep, c.st), "event");  // B and h ready
+    std::vector<std::unique_ptr<Runner>> SR(M);
+    {
+        std::vector<std::exception_ptr> fail(M);
+        auto prep = [&](int st_) {
             try {
                 ck(cudaSetDevice(dev), "cudaSetDevice");
-                ck(cudaStreamWaitEvent(cs.c[k].st, cs.prep, 0), "wait");
-                Runner W(R, cs.c[k], local[k]);
-                jobs[k](W);
+                ck(cudaStreamWaitEvent(ps.c[st_].st, ps.prep, 0), "wait");
+                SR[st_].reset(new Runner(R, ps.c[st_], acc));
+                SR[st_]->prepare_state(st_);
             } catch (...) {
-                fail[k] = std::current_exception();
+                fail[st_] = std::current_exception();
             }
-            cudaEventRecord(cs.done[k], cs.c[k].st);
+            cudaEventRecord(ps.done[st_], ps.c[st_].st);
         };
         std::vector<std::thread> th;
-        for (size_t k = 1; k < nj; ++k) th.emplace_back(work, k);
-        if (nj) work(0);
+        for (int st_ = 1; st_ < M; ++st_) th.emplace_back(prep, st_);
+        prep(0);
         for (auto &t : th) t.join();
-        for (size_t k = 0; k < nj; ++k) ck(cudaStreamWaitEvent(c.st, cs.done[k], 0), "wait");
-        for (size_t k = 0; k < nj; ++k)
-            if (fail[k]) std::rethrow_exception(fail[k]);
-        for (size_t k = 0; k < nj; ++k) acc.merge(local[k]);
+        for (int st_ = 0; st_ < M; ++st_)
+            if (fail[st_]) std::rethrow_exception(fail[st_]);
     }
+    for (int st_ = 0; st_ < M; ++st_)
+        for (int k = 0; k < norb; ++k) epsnew[k + (size_t)norb * st_] = SR[st_]->eps[k];
+    {
+        const size_t nt = (size_t)M * nj;
+        std::vector<Accum> local(nt, Accum(M));
+        std::vector<std::exception_ptr> fail(nt);
+        auto work = [&](size_t idx) {
+            const size_t st_ = idx / nj, k = idx % nj;
+            try {
+                ck(cudaSetDevice(dev), "cudaSetDevice");
+                ck(cudaStreamWaitEvent(cs.c[idx].st, ps.done[st_], 0), "wait");
+                Runner W(*SR[st_], cs.c[idx], local[idx]);
+                jobs[k](W);
+            } catch (...) {
+                fail[idx] = std::current_exception();
+            }
+            cudaEventRecord(cs.done[idx], cs.c[idx].st);
+        };
+        std::vector<std::thread> th;
+        for (size_t idx = 1; idx < nt; ++idx) th.emplace_back(work, idx);
+        if (nt) work(0);
+        for (auto &t : th) t.join();
+        for (size_t idx = 0; idx < nt; ++idx) {
+            ck(cudaStreamWaitEvent(c.st, cs.done[idx], 0), "wait");
+            // the state tensors are freed on their prepare stream: after their readers
+            ck(cudaStreamWaitEvent(ps.c[idx / nj].st, cs.done[idx], 0), "wait");
+        }
+        for (size_t idx = 0; idx < nt; ++idx)
+            if (fail[idx]) std::rethrow_exception(fail[idx]);
+        for (size_t idx = 0; idx < nt; ++idx) acc.merge(local[idx]);
+    }
+    SR.clear();
     ck(cudaStreamSynchronize(c.st), "qdnevpt sync");
     auto put = [](double *dst, const std::vector<double> &v) {
         if (dst) std::memcpy(dst, v.data(), sizeof(double) * v.size());

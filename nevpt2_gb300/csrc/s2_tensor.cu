@@ -253,6 +253,58 @@ void eigh_upper(Ctx &c, const double *A, long long n, double *w, double *V) {
     // eigenvector k as column k (column-major) = row k of the row-major array.
 }
 
+__global__ void k_add_diag(double *A, long long n, double v) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) A[i * n + i] += v;
+}
+
+bool metric_above(Ctx &c, const double *A, long long n, double thr) {
+    if (n == 0) return true;
+    double *M = nullptr, *work = nullptr;
+    int *info = nullptr;
+    ck(cudaMallocAsync((void **)&M, sizeof(double) * (size_t)(n * n), c.st), "cudaMallocAsync");
+    symmetrize_upper(c, A, n, M);
+    k_add_diag<<<nblk(n), TPB, 0, c.st>>>(M, n, -thr);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    int lwork = 0;
+    ck(cusolverDnDpotrf_bufferSize(c.sol, CUBLAS_FILL_MODE_UPPER, (int)n, M, (int)n, &lwork), "potrf_bufferSize");
+    ck(cudaMallocAsync((void **)&work, sizeof(double) * (size_t)(lwork > 0 ? lwork : 1), c.st), "cudaMallocAsync");
+    ck(cudaMallocAsync((void **)&info, sizeof(int), c.st), "cudaMallocAsync");
+    ck(cusolverDnDpotrf(c.sol, CUBLAS_FILL_MODE_UPPER, (int)n, M, (int)n, work, lwork, info), "potrf");
+    int hinfo = -1;
+    ck(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, c.st), "info copy");
+    ck(cudaStreamSynchronize(c.st), "potrf sync");
+    cudaFreeAsync(work, c.st);
+    cudaFreeAsync(info, c.st);
+    cudaFreeAsync(M, c.st);
+    return hinfo == 0;
+}
+
+bool sygvd_upper(Ctx &c, const double *K, const double *S, long long n, double *w, double *V) {
+    if (n == 0) return true;
+    double *B = nullptr, *work = nullptr;
+    int *info = nullptr;
+    symmetrize_upper(c, K, n, V);
+    ck(cudaMallocAsync((void **)&B, sizeof(double) * (size_t)(n * n), c.st), "cudaMallocAsync");
+    symmetrize_upper(c, S, n, B);
+    int lwork = 0;
+    ck(cusolverDnDsygvd_bufferSize(c.sol, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER,
+                                   (int)n, V, (int)n, B, (int)n, w, &lwork),
+       "sygvd_bufferSize");
+    ck(cudaMallocAsync((void **)&work, sizeof(double) * (size_t)(lwork > 0 ? lwork : 1), c.st), "cudaMallocAsync");
+    ck(cudaMallocAsync((void **)&info, sizeof(int), c.st), "cudaMallocAsync");
+    ck(cusolverDnDsygvd(c.sol, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, (int)n, V,
+                        (int)n, B, (int)n, w, work, lwork, info),
+       "sygvd");
+    int hinfo = -1;
+    ck(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, c.st), "info copy");
+    ck(cudaStreamSynchronize(c.st), "sygvd sync");
+    cudaFreeAsync(work, c.st);
+    cudaFreeAsync(info, c.st);
+    cudaFreeAsync(B, c.st);
+    return hinfo == 0;
+}
+
 void build_ee2L(Ctx &c, const double *taa, const double *dal, int n, double *out) {
     long long N = (long long)n * n * n * n;
     k_ee2L<<<nblk(N), TPB, 0, c.st>>>(taa, dal, n, out);

@@ -104,6 +104,13 @@ void gemm_batched(Ctx &c, bool ta, bool tb, long long m, long long n, long long 
 // col) is held in A (n x n, row-major), as dsyev('V','U') of the reference
 // sees it.  w ascending; V[k][i] = component i of eigenvector k.
 void eigh_upper(Ctx &c, const double *A, long long n, double *w, double *V);
+// True if every eigenvalue of the symmetric matrix (upper triangle of A) is
+// above thr: a Cholesky factorisation of A - thr I succeeds.
+bool metric_above(Ctx &c, const double *A, long long n, double thr);
+// Generalised symmetric-definite eigenproblem K v = w S v (upper triangles;
+// cusolverDnDsygvd): w ascending, V[k][i] = component i of eigenvector k,
+// eigenvectors S-orthonormal.  False if S is not positive definite.
+bool sygvd_upper(Ctx &c, const double *K, const double *S, long long n, double *w, double *V);
 // Symmetric copy: out = triu(A) + triu(A,1)^T.
 void symmetrize_upper(Ctx &c, const double *A, long long n, double *out);
 

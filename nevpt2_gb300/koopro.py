@@ -66,6 +66,15 @@ def ord8(nact: int, tuples) -> tuple[np.ndarray, np.ndarray]:
     return out, lind
 
 
+def ord9(nact: int, tuples) -> tuple[np.ndarray, np.ndarray]:
+    """src/ord_utils.F90:16 ord9 on the device (same conventions as ord8)."""
+    t = np.ascontiguousarray(tuples, dtype=np.int64).reshape(-1, 8)
+    out = np.zeros_like(t)
+    lind = np.zeros(t.shape[0], np.int64)
+    context().call("nvpt_ord9", nact, t.shape[0], ptr(t), ptr(out), ptr(lind))
+    return out, lind
+
+
 def bro3(ro4, nact: int, nele: int, metat: int) -> np.ndarray:
     """src/koopro4QD.F90:4881 bro3 -> daaa(metat, n^6)."""
     out = _z(metat, *(nact,) * 6)
@@ -152,3 +161,41 @@ def koopro4QD(problem) -> dict:
     out["cmatIP"], out["cmatEA"] = bcmat(atwo, daaa, taa, dal, n, nc, f, aj, M)
     out["dmatIP"], out["dmatEA"] = bdmat(atwo, taa, dal, n, nc, f, aj, M)
     return out
+
+
+def permute_4rdm(ro4, labels, values):
+    """src/rdm_utils.F90:236 permute_4rdm over a QCMaquis label/value list
+    (as hdf5_read_rdm_from_resfile applies it): ``ro4`` (W,n,n,n,n) of one
+    state, Fortran order, updated in place; ``labels`` (nentries, 8) 0-based."""
+    n = ro4.shape[1]
+    lab = np.ascontiguousarray(labels, dtype=np.int32)
+    val = np.ascontiguousarray(values, dtype=np.float64)
+    if not ro4.flags.f_contiguous:
+        raise ValueError("ro4 must be Fortran-contiguous")
+    context().call("nvpt_permute_4rdm", ptr(ro4), n, ptr(lab), ptr(val), val.size)
+    return ro4
+
+
+def permute_3rdm(rdm3, labels, values, trans: bool = False, state: int = 0):
+    """src/rdm_utils.F90:470 permute_3rdm into ``rdm3`` -- (M,n,n,n,n,n,n)
+    Fortran order (state ``state``) or (n,)*6 -- in place; ``labels``
+    (nentries, 6) 0-based."""
+    if not rdm3.flags.f_contiguous:
+        raise ValueError("rdm3 must be Fortran-contiguous")
+    if rdm3.ndim == 7:
+        ld, n = rdm3.shape[0], rdm3.shape[1]
+        flat = rdm3.reshape(-1, order="F")
+        base = flat[state:]
+    else:
+        ld, n = 1, rdm3.shape[0]
+        base = rdm3.reshape(-1, order="F")
+    lab = np.ascontiguousarray(labels, dtype=np.int32)
+    val = np.ascontiguousarray(values, dtype=np.float64)
+    # the host entry stages ld * n^6 elements from the pointer: hand it a
+    # buffer of exactly that extent
+    tmp = np.zeros(ld * n**6)
+    tmp[: base.size] = base
+    context().call("nvpt_permute_3rdm", ptr(tmp), ld, n, ptr(lab), ptr(val), val.size, int(trans))
+    base[:] = tmp[: base.size]
+    return rdm3
+

@@ -47,6 +47,8 @@ class Stage1:
             self.out[k] = z(M * n**4)
         for k in self.OUTPUTS_N6:
             self.out[k] = z(M * n**6)
+        # transition RDMs of the root pairs (quasi-degenerate stage 2)
+        self.trdm = tuple(_dev(t, self.device) for t in p.trdm) if (M > 1 and p.trdm is not None) else None
 
     def run(self, stream: torch.cuda.Stream | None = None) -> None:
         """Enqueue the whole stage on ``stream`` (default: torch's current)."""
@@ -72,13 +74,13 @@ class Stage1:
 
     def stage2(self, stream: torch.cuda.Stream | None = None, thr_lindep: float = 1e-6, class_mask: int = 0xFF):
         """Run the NEVPT2 energy stage on the resident stage-1 outputs
-        (nvpt_qdnevpt_d; single-state problems, no transition RDMs)."""
+        (nvpt_qdnevpt_d), with the resident transition RDMs when metat > 1."""
         import ctypes
 
         from . import qdnevpt as gq
         p, o = self.p, self.out
-        if p.metat != 1:
-            raise NotImplementedError("resident stage 2 runs single-state problems; use qdnevpt.qdnevpt for QD")
+        if p.metat > 1 and self.trdm is None:
+            raise ValueError("a multi-state problem needs its transition RDMs (Problem.trdm)")
         gq._bind(self.ctx)
         st = ptr_stream(stream or torch.cuda.current_stream(self.device))
         inp = gq._In(p.ncore, p.nact, p.nvirt, p.metat, p.chol.shape[0], thr_lindep, 0, class_mask, None,
@@ -86,7 +88,7 @@ class Stage1:
                      ptr(o["1-IPKO"]), ptr(o["1-EAKO"]), ptr(o["2-IPKO"]), ptr(o["2-EAKO"]), ptr(o["gk0pa"]),
                      ptr(o["gk0pd"]), ptr(o["gk0pf"]), ptr(o["amatIP"]), ptr(o["amatEA"]), ptr(o["bmatIP"]),
                      ptr(o["bmatEA"]), ptr(o["cmatIP"]), ptr(o["cmatEA"]), ptr(o["dmatIP"]), ptr(o["dmatEA"]),
-                     None, None, None)
+                     *((ptr(t) for t in self.trdm) if self.trdm is not None else (None, None, None)))
         M = p.metat
         res = gq.Stage2Energies(*(np.zeros((8, M), order="F") for _ in range(4)), np.zeros((M, M), order="F"),
                                 np.zeros((M, M), order="F"), np.zeros(M), np.zeros(M),

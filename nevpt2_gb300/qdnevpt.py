@@ -81,6 +81,8 @@ def qdnevpt(problem, koop: dict, transition=None, thr_lindep: float = 1e-6, clas
     _bind(ctx)
     p = problem
     M, n = p.metat, p.nact
+    if transition is None and M > 1:
+        transition = getattr(p, "trdm", None)
     keep = []
 
     def h(a):

@@ -92,6 +92,8 @@ class Problem:
     chol: np.ndarray          # (Q, npair) Fortran order
     eps: np.ndarray           # target orbital energies (norb,)
     energies: np.ndarray = field(default_factory=lambda: np.zeros(1))
+    # transition 1-3-RDMs (daoff, daaoff, ro3off) of every root pair, metat > 1
+    trdm: tuple | None = None
 
     @property
     def norb(self) -> int:
@@ -160,7 +162,8 @@ def fock_two_electron(L: np.ndarray, norb: int, ncore: int, nact: int, gamma1: n
 
 
 def make_problem(nact: int, nele: int, ncore: int, nvirt: int, metat: int = 1, ndet: int | None = None,
-                 seed: int = 20261203, nchovec: int | None = None, with_ro4: bool = True) -> Problem:
+                 seed: int = 20261203, nchovec: int | None = None, with_ro4: bool = True,
+                 with_trdm: bool = False) -> Problem:
     """Build one seeded problem.  ``ndet=None`` takes the full CAS space."""
     if nact > 16:
         raise ValueError("nact <= 16")
@@ -184,9 +187,10 @@ def make_problem(nact: int, nele: int, ncore: int, nvirt: int, metat: int = 1, n
     G = fock_two_electron(chol, norb, ncore, nact, dal[0])
     h1 = F - G
     oneint = np.array([h1[p, q] for p in range(norb) for q in range(p + 1)])
+    trdm = transition_rdms(n, amask, bmask, coef) if (with_trdm and metat > 1) else None
     return Problem(nact=n, nele=nele, ncore=ncore, nvirt=nvirt, metat=metat, nchovec=Q, seed=seed, amask=amask,
                    bmask=bmask, coef=coef, dal=dal, taa=taa, daaa=daaa, ro4=ro4, oneint=oneint, chol=chol, eps=eps,
-                   energies=np.zeros(metat))
+                   energies=np.zeros(metat), trdm=trdm)
 
 
 def rdms(n: int, amask, bmask, coef, with_ro4: bool = True):
@@ -254,5 +258,6 @@ CONFIGS = {
 
 def config_problem(name: str, **over) -> Problem:
     kw = dict(CONFIGS[name])
+    kw.setdefault("with_trdm", kw["metat"] > 1)
     kw.update(over)
     return make_problem(**kw)

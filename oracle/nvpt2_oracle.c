@@ -941,3 +941,163 @@ int orc_num_threads(void) {
     return 1;
 #endif
 }
+
+/* ------------------------------------------------------------------------
+ * rdm_utils.F90:236-464 permute_4rdm and :470-511 permute_3rdm, applied as
+ * hdf5_read_rdm_from_resfile (:193-226) does: labels (0-based, as stored)
+ * + 1, one call per entry in file order, every image an assignment.
+ * Transcribed branch for branch from the reference (including its
+ * redundant branches); DUMP4 is its dump_element macro.
+ * ------------------------------------------------------------------------ */
+#define DUMP4(v, a, b, cc, d) \
+    ro4[(o_norm(i, j, k, l) - 1) + W * (((a)-1) + n_ * (((b)-1) + n_ * (((cc)-1) + n_ * ((d)-1))))] = (v)
+
+static void o_permute_4rdm(double *ro4, I n_, I W, I i, I j, I k, I l, I m, I n, I o, I p, double val) {
+    const double thresh = 1.0e-12;
+    if (fabs(val) < thresh) return;
+    double valm05 = val * (-0.5), valm2 = val * (-2.0);
+    if ((i == j) && (k == l)) {
+        if ((m == n) && (o == p)) {
+            DUMP4(val, m, n, o, o); DUMP4(val, o, o, m, m);
+            DUMP4(valm05, m, o, o, m); DUMP4(valm05, m, o, m, o); DUMP4(valm05, o, m, m, o); DUMP4(valm05, o, m, o, m);
+        } else {
+            if ((m == n) && (o != p)) {
+                DUMP4(val, m, n, o, p);
+                DUMP4(val, m, m, p, o); DUMP4(val, o, p, m, m); DUMP4(val, p, o, m, m);
+                DUMP4(valm05, o, m, m, p); DUMP4(valm05, o, m, p, m); DUMP4(valm05, p, m, m, o);
+                DUMP4(valm05, p, m, o, m); DUMP4(valm05, m, o, p, m); DUMP4(valm05, m, p, o, m);
+                DUMP4(valm05, m, p, m, o); DUMP4(valm05, m, o, m, p);
+            } else {
+                if ((m != n) && (o == p)) {
+                    DUMP4(val, m, n, o, p);
+                    DUMP4(val, n, m, o, o); DUMP4(val, o, o, m, n); DUMP4(val, o, o, n, m);
+                    DUMP4(valm05, m, o, o, n); DUMP4(valm05, n, o, o, m); DUMP4(valm05, o, m, o, n);
+                    DUMP4(valm05, o, n, o, m); DUMP4(valm05, o, m, n, o); DUMP4(valm05, o, n, m, o);
+                    DUMP4(valm05, m, o, n, o); DUMP4(valm05, n, o, m, o);
+                } else {
+                    if ((m != n) && (o != p)) {
+                        if (n == o) {
+                            DUMP4(val, m, n, o, p);
+                            DUMP4(valm2, n, n, m, p); DUMP4(valm2, n, n, p, m); DUMP4(valm2, m, p, n, n);
+                            DUMP4(valm2, p, m, n, n);
+                            DUMP4(val, p, n, n, m); DUMP4(val, p, n, m, n); DUMP4(val, m, n, p, n);
+                            DUMP4(val, n, p, m, n); DUMP4(val, n, m, p, n); DUMP4(val, n, m, n, p);
+                            DUMP4(val, n, p, n, m);
+                        } else {
+                            if ((n < o) && (p != m)) {
+                                DUMP4(val, m, n, o, p);
+                                DUMP4(val, m, n, p, o); DUMP4(val, n, m, p, o); DUMP4(val, n, m, o, p);
+                                DUMP4(val, o, p, m, n); DUMP4(val, o, p, n, m); DUMP4(val, p, o, n, m);
+                                DUMP4(val, p, o, m, n);
+                            } else {
+                                if (o != p) {
+                                    DUMP4(val, m, n, o, p); DUMP4(val, m, n, p, o); DUMP4(val, n, m, p, o);
+                                    DUMP4(val, n, m, o, p); DUMP4(val, o, p, m, n); DUMP4(val, o, p, n, m);
+                                    DUMP4(val, p, o, n, m); DUMP4(val, p, o, m, n);
+                                }
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    } else {
+        if ((i == j) && (k != l)) {
+            if ((m == n) && (o == p)) {
+                DUMP4(val, m, n, o, p); DUMP4(val, o, o, m, m);
+                DUMP4(valm05, m, o, o, m); DUMP4(valm05, o, m, m, o); DUMP4(valm05, o, m, o, m);
+                DUMP4(valm05, m, o, m, o);
+            }
+            if ((m == n) && (o != p)) {
+                DUMP4(val, m, n, o, p);
+                DUMP4(valm05, m, o, m, p); DUMP4(valm05, m, p, o, m); DUMP4(valm05, o, m, m, p);
+                DUMP4(valm05, p, m, o, m);
+            }
+            if ((m != n) && (o == p)) { DUMP4(val, m, n, o, p); DUMP4(val, n, m, o, o); }
+            if ((m != n) && (n != o) && (o != p) && (m != p)) { DUMP4(val, m, n, o, p); DUMP4(val, n, m, o, p); }
+        } else {
+            if ((i != j) && (j == k) && (k != l)) {
+                if ((m == n) && (o == p)) {
+                    DUMP4(val, m, n, o, p); DUMP4(val, o, o, m, m); DUMP4(val, o, m, o, m); DUMP4(val, m, o, m, o);
+                    DUMP4(valm2, m, o, o, m); DUMP4(valm2, o, m, m, o);
+                }
+                if ((m != n) && (o == p)) {
+                    DUMP4(val, m, n, o, p); DUMP4(val, o, o, m, n); DUMP4(val, o, m, o, n); DUMP4(val, m, o, n, o);
+                    DUMP4(valm2, m, o, o, n);
+                }
+                if ((m != n) && (o != p) && (m == p)) { DUMP4(val, m, n, o, p); DUMP4(val, m, o, n, m); }
+                if ((m != n) && (n != o) && (o != p) && (m != p)) { DUMP4(val, m, n, o, p); DUMP4(val, m, o, n, p); }
+            } else {
+                if ((i != j) && (k == l)) {
+                    if ((m == n) && (o == p)) {
+                        DUMP4(val, m, n, o, p); DUMP4(val, o, o, m, m);
+                        DUMP4(valm05, m, o, o, m); DUMP4(valm05, o, m, m, o); DUMP4(valm05, o, m, o, m);
+                        DUMP4(valm05, m, o, m, o);
+                    }
+                    if ((m == n) && (o != p)) { DUMP4(val, m, n, o, p); DUMP4(val, m, m, p, o); }
+                    if ((m != n) && (o == p)) {
+                        DUMP4(val, m, n, o, p);
+                        DUMP4(valm05, m, o, n, o); DUMP4(valm05, m, o, o, n); DUMP4(valm05, o, n, o, m);
+                        DUMP4(valm05, o, n, m, o);
+                    }
+                    if ((m != n) && (n != o) && (o != p) && (m != p)) { DUMP4(val, m, n, o, p); DUMP4(val, m, n, p, o); }
+                } else {
+                    if ((i != j) && (k != l) && (j != k)) {
+                        if (((m == o) && (n == p)) || ((m == p) && (n == o))) {
+                            DUMP4(val, m, n, o, p); DUMP4(val, n, m, p, o);
+                        } else {
+                            if ((m == n) && (o == p)) { DUMP4(val, m, n, o, p); DUMP4(val, o, o, m, m); }
+                            else { DUMP4(val, m, n, o, p); }
+                        }
+                    }
+                }
+            }
+        }
+    }
+}
+#undef DUMP4
+
+/* labels: 8 x nentries (int32, 0-based, label-major); ro4: (W,n,n,n,n) of one state.
+ * Returns 1 if a label is out of range (nothing written for it), else 0. */
+int orc_permute_4rdm(double *ro4, I nact, const int32_t *labels, const double *values, I nentries) {
+    const I W = nact * (nact + 1) * (nact + 2) * (nact + 3) / 24;
+    int bad = 0;
+    for (I e = 0; e < nentries; ++e) {
+        const int32_t *L = labels + 8 * e;
+        int ok = 1;
+        for (int t = 0; t < 8; ++t) ok &= (L[t] >= 0 && L[t] < nact);
+        if (!ok) { bad = 1; continue; }
+        o_permute_4rdm(ro4, nact, W, L[0] + 1, L[1] + 1, L[2] + 1, L[3] + 1, L[4] + 1, L[5] + 1, L[6] + 1, L[7] + 1,
+                       values[e]);
+    }
+    return bad;
+}
+
+/* labels: 6 x nentries; rdm3 element (i..n) (1-based) at rdm3[ld * ((i-1) + n ((j-1) + ...))]. */
+int orc_permute_3rdm(double *rdm3, I ld, I nact, const int32_t *labels, const double *values, I nentries,
+                     int trans) {
+    const I n_ = nact;
+    int bad = 0;
+#define DUMP3(v, a, b, cc, d, e, f)                                                                              \
+    rdm3[ld * (((a)-1) + n_ * (((b)-1) + n_ * (((cc)-1) + n_ * (((d)-1) + n_ * (((e)-1) + n_ * ((f)-1))))))] = (v)
+    for (I e = 0; e < nentries; ++e) {
+        const int32_t *L = labels + 6 * e;
+        int ok = 1;
+        for (int t = 0; t < 6; ++t) ok &= (L[t] >= 0 && L[t] < nact);
+        if (!ok) { bad = 1; continue; }
+        I i = L[0] + 1, j = L[1] + 1, k = L[2] + 1, l = L[3] + 1, m = L[4] + 1, n = L[5] + 1;
+        double val = values[e];
+        double tmp = trans ? val : -val;
+        if (fabs(val) < 1.0e-12) continue;
+        if ((i == j) && (i == k)) continue;
+        if ((l == m) && (l == n)) continue;
+        DUMP3(tmp, i, j, k, l, m, n); DUMP3(tmp, i, k, j, l, n, m); DUMP3(tmp, j, i, k, m, l, n);
+        DUMP3(tmp, j, k, i, m, n, l); DUMP3(tmp, k, i, j, n, l, m); DUMP3(tmp, k, j, i, n, m, l);
+        if (!trans) {
+            DUMP3(tmp, l, m, n, i, j, k); DUMP3(tmp, l, n, m, i, k, j); DUMP3(tmp, m, l, n, j, i, k);
+            DUMP3(tmp, m, n, l, j, k, i); DUMP3(tmp, n, l, m, k, i, j); DUMP3(tmp, n, m, l, k, j, i);
+        }
+    }
+#undef DUMP3
+    return bad;
+}

@@ -39,6 +39,9 @@ def lib():
         L.orc_ai.argtypes = [P, I64, I64, I64, I64, I64]; L.orc_ai.restype = ctypes.c_double
         L.orc_get_aj_atwo.argtypes = [P, P, I64, I64, I64, I64, P, P]
         L.orc_koop_matrices_ctl.argtypes = [I64, I64, I64] + [P] * 14
+        L.orc_permute_4rdm.argtypes = [P, I64, P, P, I64]; L.orc_permute_4rdm.restype = ctypes.c_int
+        L.orc_permute_3rdm.argtypes = [P, I64, I64, P, P, I64, ctypes.c_int]
+        L.orc_permute_3rdm.restype = ctypes.c_int
         L.orc_fdiff_F.argtypes = [P, I64, I64, P]
         L.orc_bamat.argtypes = [P] * 7 + [I64, I64, P, P, I64, I64]
         L.orc_bamat_slabs.argtypes = [P] * 7 + [I64, I64, P, P, I64, I64]
@@ -192,3 +195,21 @@ def stage1(problem):
     out["cmatIP"], out["cmatEA"] = bcmat(atwo, p.daaa, p.taa, p.dal, n, nc, f, aj, M)
     out["dmatIP"], out["dmatEA"] = bdmat(atwo, p.taa, p.dal, n, nc, f, aj, M)
     return out
+
+
+def permute_4rdm(ro4, labels, values):
+    """rdm_utils.F90:236 permute_4rdm over a label list, sequentially (C)."""
+    lab = np.ascontiguousarray(labels, dtype=np.int32)
+    val = np.ascontiguousarray(values, dtype=np.float64)
+    assert ro4.flags.f_contiguous
+    bad = lib().orc_permute_4rdm(_p(ro4), ro4.shape[1], _p(lab), _p(val), val.size)
+    return ro4, bad
+
+
+def permute_3rdm(flat, ld, n, labels, values, trans=False):
+    """rdm_utils.F90:470 permute_3rdm into a flat buffer with element stride ld."""
+    lab = np.ascontiguousarray(labels, dtype=np.int32)
+    val = np.ascontiguousarray(values, dtype=np.float64)
+    bad = lib().orc_permute_3rdm(_p(flat), ld, n, _p(lab), _p(val), val.size, int(trans))
+    return flat, bad
+

@@ -252,11 +252,13 @@ class _State:
         Ja = np.einsum("xab,ba->x", B[:, act, act], g1)
 
         def fock(sl):
+            # the same sums as the reference's loops, grouped into BLAS calls
             F = h[sl, sl].copy()
-            F += 2.0 * np.einsum("xpq,x->pq", B[:, sl, sl], Jc)
-            F -= np.einsum("xpk,xkq->pq", B[:, sl, core], B[:, core, sl])
-            F += np.einsum("xpq,x->pq", B[:, sl, sl], Ja)
-            F -= 0.5 * np.einsum("xpb,ba,xaq->pq", B[:, sl, act], g1, B[:, act, sl])
+            Bss = B[:, sl, sl]
+            F += 2.0 * np.tensordot(Jc, Bss, axes=(0, 0))
+            F -= np.tensordot(B[:, sl, core], B[:, core, sl], axes=([0, 2], [0, 1]))
+            F += np.tensordot(Ja, Bss, axes=(0, 0))
+            F -= 0.5 * np.tensordot(np.matmul(B[:, sl, act], g1), B[:, act, sl], axes=([0, 2], [0, 1]))
             return F
 
         eps = np.zeros(norb)
@@ -276,7 +278,11 @@ class _State:
         U[act, act] = np.eye(na)
         U[virt, virt] = Uv
         # transformed DF vectors (virtual-virtual block is never formed)
-        R = np.einsum("pi,xpq,qj->xij", U, B, U, optimize=True)
+        # R[x] = U^T B[x] U as two large GEMMs
+        Q = B.shape[0]
+        T1 = (B.reshape(Q * norb, norb) @ U).reshape(Q, norb, norb)
+        T2 = U.T @ T1.transpose(1, 0, 2).reshape(norb, Q * norb)
+        R = np.ascontiguousarray(T2.reshape(norb, Q, norb).transpose(1, 0, 2))
         R[:, virt, virt] = 0.0
         self.R = R
         self.h = U.T @ h @ U
@@ -287,9 +293,15 @@ class _State:
         return np.einsum("xab,xcd->abcd", self.R[:, a, b], self.R[:, c, d], optimize=True)
 
 
-def qdnevpt(inp: Stage2Inputs, classes=range(8), pc=True) -> Stage2Result:
+def qdnevpt(inp: Stage2Inputs, classes=range(8), pc=True, timings: dict | None = None) -> Stage2Result:
     """Stage 2 for every state (src/qdnevpt.F:858-993) plus the per-class
-    bookkeeping of the energies and norms."""
+    bookkeeping of the energies and norms.  ``timings``, if given, collects
+    the wall time of the per-state setup ("setup") and of each class (0-7)."""
+    import time as _time
+
+    def tick(key, t0):
+        if timings is not None:
+            timings[key] = timings.get(key, 0.0) + _time.perf_counter() - t0
     M = inp.metat
     nc, na, nv, norb = inp.ncore, inp.nact, inp.nvirt, inp.norb
     B = dense_B(inp.chol, norb)
@@ -301,24 +313,20 @@ def qdnevpt(inp: Stage2Inputs, classes=range(8), pc=True) -> Stage2Result:
     for k in inp.frozen:
         fro[k] = True
     for s in range(M):
+        t0 = _time.perf_counter()
         st = _State(inp, s, B, h)
         r.epsnew[:, s] = st.eps
-        if 0 in classes:
-            _v0(inp, st, s, r, fro)
-        if 1 in classes:
-            _v1k(inp, st, s, r, fro, pc)
-        if 2 in classes:
-            _vm1k(inp, st, s, r, fro, pc)
-        if 3 in classes:
-            _v2mod(inp, st, s, r, fro, pc)
-        if 4 in classes:
-            _vm2mod(inp, st, s, r, fro, pc)
-        if 7 in classes:
-            _v0pmod(inp, st, s, r, fro, pc)
-        if 6 in classes:
-            _vmupE(inp, st, s, r, fro, pc)
-        if 5 in classes:
-            _vpupE(inp, st, s, r, fro, pc)
+        tick("setup", t0)
+        for c, fn in ((0, None), (1, _v1k), (2, _vm1k), (3, _v2mod), (4, _vm2mod), (7, _v0pmod), (6, _vmupE),
+                      (5, _vpupE)):
+            if c not in classes:
+                continue
+            t0 = _time.perf_counter()
+            if c == 0:
+                _v0(inp, st, s, r, fro)
+            else:
+                fn(inp, st, s, r, fro, pc)
+            tick(c, t0)
     return r
 
 

@@ -35,6 +35,21 @@ def test_ord8_bit_exact_n16_sample(gpu_ctx):
     np.testing.assert_array_equal(got, orc.ord_tuples(16, 8, t))
 
 
+def test_ord9_bit_exact_all_tuples_and_n16_sample(gpu_ctx):
+    n = 4
+    t = np.array(list(itertools.product(range(1, n + 1), repeat=8)), dtype=np.int64)
+    got, lind = koopro.ord9(n, t)
+    ref = orc.ord_tuples(n, 9, t)
+    np.testing.assert_array_equal(got, ref)
+    lindi, lindj, lindk, _ = orc.index_tables(n)
+    np.testing.assert_array_equal(lind, lindi[ref[:, 0] - 1] + lindj[ref[:, 1] - 1] + lindk[ref[:, 2] - 1] + ref[:, 3])
+    rng = np.random.default_rng(2)
+    t = rng.integers(1, 17, (100000, 8)).astype(np.int64)
+    t[::2, 4:] = t[::2, :4][:, ::-1]
+    got, _ = koopro.ord9(16, t)
+    np.testing.assert_array_equal(got, orc.ord_tuples(16, 9, t))
+
+
 @pytest.mark.parametrize("n,ne,metat,ndet", [(6, 6, 2, None), (8, 8, 1, None), (7, 5, 1, 200)])
 def test_bro_chain(gpu_ctx, n, ne, metat, ndet):
     p = synth.make_problem(n, ne, 2, 3, metat=metat, ndet=ndet, seed=31)
