@@ -398,6 +398,26 @@ def run_ours(args):
     clk = clocks.stop()
     bamat_ms = bamat_alone()
 
+    # FP64 rounding floor of the energies: the same stage 2 after multiplying
+    # every A-matrix element by (1 + 2^-52 xi), xi ~ N(0,1) -- a perturbation the
+    # size of one rounding of each element.  Energy differences of this size
+    # are FP64 noise for the problem at hand.
+    def ulp_sensitivity():
+        g = torch.Generator(device=dev)
+        g.manual_seed(11)
+        saved = {k: st.out[k].clone() for k in ("amatIP", "amatEA")}
+        for k, x in saved.items():
+            st.out[k].mul_(1 + 2.0**-52 * torch.randn(x.shape, dtype=x.dtype, device=dev, generator=g))
+        with torch.cuda.stream(stream):
+            e1 = st.stage2(stream)
+        torch.cuda.synchronize(dev)
+        for k in saved:
+            st.out[k].copy_(saved[k])
+        return {"per_class_pc_max": float(np.abs(e1.e2enp - energies.e2enp).max()),
+                "per_class_sc_max": float(np.abs(e1.e2mpp - energies.e2mpp).max())}
+
+    fp64_floor = ulp_sensitivity()
+
     # ---------------- split precision (Ozaki digits on tcgen05) ----------------
     set_mode(koopro.SPLIT)
     with torch.cuda.stream(stream):
@@ -487,6 +507,7 @@ def run_ours(args):
                                         "total_sc": de(e_sp.e2mp, energies.e2mp),
                                         "total_pc": de(e_sp.e2en, energies.e2en)},
                       "nnew_equal": bool(np.array_equal(e_sp.nnew, energies.nnew)),
+                      "fp64_one_ulp_floor_eh": fp64_floor,
                       "roofline": {"kernel": "k_oz_gemm (Ozaki digit products, tcgen05)", "bound": "hbm",
                                    "achieved": oz_gbs, "peak": hbm_peak, "unit": "GB/s",
                                    "frac": (oz_gbs / hbm_peak) if oz_gbs else None, "traffic": None,
