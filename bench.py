@@ -418,6 +418,26 @@ def run_ours(args):
 
     fp64_floor = ulp_sensitivity()
 
+    # device time of the stage-2 pieces in one FP64 step (spans on the pieces'
+    # own streams; they overlap in time, so they do not add up to the step)
+    S2_TAGS = ["s2_prepare", "s2_class_0", "s2_class_+1", "s2_class_-1", "s2_class_+2", "s2_class_-2",
+               "s2_class_0p", "s2_class_+1p", "s2_class_-1p"]
+
+    def stage2_breakdown():
+        ctx.call("nvpt_set_profiling", 1)
+        with torch.cuda.stream(stream):
+            st.stage2(stream)
+        torch.cuda.synchronize(dev)
+        out = {}
+        for tag in S2_TAGS:
+            t_ms, t_n, t_b = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
+            ctx.call("nvpt_profile_read", tag.encode(), ctypes.byref(t_ms), ctypes.byref(t_n), ctypes.byref(t_b))
+            out[tag] = round(t_ms.value, 2)
+        ctx.call("nvpt_set_profiling", 0)
+        return out
+
+    s2_breakdown = stage2_breakdown()
+
     # ---------------- split precision (Ozaki digits on tcgen05) ----------------
     set_mode(koopro.SPLIT)
     with torch.cuda.stream(stream):
@@ -514,6 +534,7 @@ def run_ours(args):
                                    "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
                                    "kernel_ms": oz_ms.value, "launches": oz_n.value, "alg_bytes": oz_bytes.value},
                       "clocks": clk_sp, "step_ms_all": times_sp},
+            "stage2_ms_per_piece": s2_breakdown,
             "energies": energy_summary(energies),
             "clocks": clk, "cpu_baseline": cb, "step_ms_all": times}
     print(json.dumps(line), flush=True)

@@ -178,7 +178,10 @@ int nvpt_get_precision(nvpt_context *ctx);
  * (process-wide), tagged launches are bracketed by CUDA events on their
  * stream; nvpt_profile_read waits for and sums the spans of one tag (total
  * ms, launch count, algorithmic bytes) and forgets them.  Tags: "oz_gemm"
- * (the split-precision product kernel). */
+ * (the split-precision product kernel), "s2_prepare" (stage-2 orbitals and
+ * transformed integrals of one state), "s2_class_0", "s2_class_+1",
+ * "s2_class_-1", "s2_class_+2", "s2_class_-2", "s2_class_0p",
+ * "s2_class_+1p", "s2_class_-1p" (one class of one state, on its stream). */
 int nvpt_set_profiling(nvpt_context *ctx, int on);
 int nvpt_profile_read(nvpt_context *ctx, const char *tag, double *ms, int64_t *launches, int64_t *bytes);
 

@@ -1577,14 +1577,15 @@ int run_qdnevpt(nvpt_context *ctx, cudaStream_t st, const nvpt_qdnevpt_in *in, n
     // (0, +1, -1, +2, -2, 0', -1', +1').
     using Job = std::function<void(Runner &)>;
     std::vector<Job> jobs;
-    if (m & 1u) jobs.push_back([](Runner &r) { r.class0(); });
-    if (m & 2u) jobs.push_back([pc](Runner &r) { r.class_pm1(true, pc); });
-    if (m & 4u) jobs.push_back([pc](Runner &r) { r.class_pm1(false, pc); });
-    if (m & 8u) jobs.push_back([pc](Runner &r) { r.class_pm2(true, pc); });
-    if (m & 16u) jobs.push_back([pc](Runner &r) { r.class_pm2(false, pc); });
-    if (m & 128u) jobs.push_back([pc](Runner &r) { r.class0p(pc); });
-    if (m & 64u) jobs.push_back([pc](Runner &r) { r.class_pm1p(true, pc); });
-    if (m & 32u) jobs.push_back([pc](Runner &r) { r.class_pm1p(false, pc); });
+    std::vector<const char *> tags;  // live-timing tags (nvpt_profile_read)
+    if (m & 1u) { jobs.push_back([](Runner &r) { r.class0(); }); tags.push_back("s2_class_0"); }
+    if (m & 2u) { jobs.push_back([pc](Runner &r) { r.class_pm1(true, pc); }); tags.push_back("s2_class_+1"); }
+    if (m & 4u) { jobs.push_back([pc](Runner &r) { r.class_pm1(false, pc); }); tags.push_back("s2_class_-1"); }
+    if (m & 8u) { jobs.push_back([pc](Runner &r) { r.class_pm2(true, pc); }); tags.push_back("s2_class_+2"); }
+    if (m & 16u) { jobs.push_back([pc](Runner &r) { r.class_pm2(false, pc); }); tags.push_back("s2_class_-2"); }
+    if (m & 128u) { jobs.push_back([pc](Runner &r) { r.class0p(pc); }); tags.push_back("s2_class_0p"); }
+    if (m & 64u) { jobs.push_back([pc](Runner &r) { r.class_pm1p(true, pc); }); tags.push_back("s2_class_+1p"); }
+    if (m & 32u) { jobs.push_back([pc](Runner &r) { r.class_pm1p(false, pc); }); tags.push_back("s2_class_-1p"); }
     const size_t nj = jobs.size();
     // The states are independent too: every state is prepared on its own
     // stream, then every (state, class) pair runs concurrently.  The
@@ -1601,7 +1602,10 @@ int run_qdnevpt(nvpt_context *ctx, cudaStream_t st, const nvpt_qdnevpt_in *in, n
                 ck(cudaSetDevice(dev), "cudaSetDevice");
                 ck(cudaStreamWaitEvent(ps.c[st_].st, ps.prep, 0), "wait");
                 SR[st_].reset(new Runner(R, ps.c[st_], acc));
+                ProfSpan span;
+                span.begin("s2_prepare", ps.c[st_].st, 0);
                 SR[st_]->prepare_state(st_);
+                span.end();
             } catch (...) {
                 fail[st_] = std::current_exception();
             }
@@ -1626,7 +1630,10 @@ int run_qdnevpt(nvpt_context *ctx, cudaStream_t st, const nvpt_qdnevpt_in *in, n
                 ck(cudaSetDevice(dev), "cudaSetDevice");
                 ck(cudaStreamWaitEvent(cs.c[idx].st, ps.done[st_], 0), "wait");
                 Runner W(*SR[st_], cs.c[idx], local[idx]);
+                ProfSpan span;
+                span.begin(tags[k], cs.c[idx].st, 0);
                 jobs[k](W);
+                span.end();
             } catch (...) {
                 fail[idx] = std::current_exception();
             }
