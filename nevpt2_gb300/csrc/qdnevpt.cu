@@ -204,7 +204,8 @@ struct State {
 T eri(Ctx &c, const T &X, const T &Y) {
     long long Q = X.sh[0], m = X.size() / Q, n = Y.size() / Q;
     T out = alloc(c, {m, n}, false);
-    gemm(c, true, false, m, n, Q, 1.0, X.p, m, Y.p, n, 0.0, out.p, n);
+    if (X.p == Y.p) gram(c, X.p, Q, m, out.p);  // (pq|rs) = (rs|pq): one triangle
+    else gemm(c, true, false, m, n, Q, 1.0, X.p, m, Y.p, n, 0.0, out.p, n);
     return out;
 }
 

@@ -258,6 +258,24 @@ __global__ void k_add_diag(double *A, long long n, double v) {
     if (i < n) A[i * n + i] += v;
 }
 
+__global__ void k_mirror_lower(double *o, long long m) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= m * m) return;
+    long long r = t / m, col = t % m;
+    if (r < col) o[t] = o[col * m + r];
+}
+
+void gram(Ctx &c, const double *X, long long Q, long long m, double *out) {
+    if (m == 0) return;
+    const double one = 1.0, zero = 0.0;
+    // column-major view: X is m x Q (ld m); C = X X^T fills the column-major
+    // upper triangle = the row-major lower triangle of out
+    ck(cublasDsyrk(c.blas, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, (int)m, (int)Q, &one, X, (int)m, &zero, out, (int)m),
+       "cublasDsyrk");
+    k_mirror_lower<<<nblk(m * m), TPB, 0, c.st>>>(out, m);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+
 bool metric_above(Ctx &c, const double *A, long long n, double thr) {
     if (n == 0) return true;
     double *M = nullptr, *work = nullptr;

@@ -104,6 +104,9 @@ void gemm_batched(Ctx &c, bool ta, bool tb, long long m, long long n, long long 
 // col) is held in A (n x n, row-major), as dsyev('V','U') of the reference
 // sees it.  w ascending; V[k][i] = component i of eigenvector k.
 void eigh_upper(Ctx &c, const double *A, long long n, double *w, double *V);
+// out[m,m] (row-major) = X^T X for X [Q, m] row-major: the symmetric rank-Q
+// update (cublasDsyrk, half the flops of a GEMM) mirrored to a full matrix.
+void gram(Ctx &c, const double *X, long long Q, long long m, double *out);
 // True if every eigenvalue of the symmetric matrix (upper triangle of A) is
 // above thr: a Cholesky factorisation of A - thr I succeeds.
 bool metric_above(Ctx &c, const double *A, long long n, double thr);
