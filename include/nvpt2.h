@@ -191,6 +191,18 @@ int nvpt_profile_read(nvpt_context *ctx, const char *tag, double *ms, int64_t *l
 int nvpt_dgemm_split_d(nvpt_context *ctx, int64_t m, int64_t n, int64_t k, const double *A, const double *B,
                        double *C, void *stream);
 
+/* The general split-precision product (no counterpart in the reference):
+ * row-major C[m,n] = alpha op(A) op(B) + beta C on device pointers, op(A) =
+ * A[m,k] (ld lda) or, with transa, A^T for A[k,m]; op(B) = B[k,n] (ld ldb)
+ * or, with transb, B^T for B[n,k].  Any m, n >= 1 and 1 <= k <= 2^19;
+ * alpha must be +-2^e (it is folded into the digit exponents).  Each term
+ * carries at most 2^-59 max|row of op(A)| max|column of op(B)| of error,
+ * at or below an FP64 dot product's rounding.  NVPT_ETIMEDOUT if the
+ * product's pipeline timed out. */
+int nvpt_dgemm_split_ex_d(nvpt_context *ctx, int transa, int transb, int64_t m, int64_t n, int64_t k, double alpha,
+                          const double *A, int64_t lda, const double *B, int64_t ldb, double beta, double *C,
+                          int64_t ldc, void *stream);
+
 /* No-allocation variant of nvpt_bamat_d -- no counterpart in the reference.
  * Same arguments and results (to rounding: its contractions sum in another
  * order), for callers that must not allocate device memory during a run:

@@ -1,6 +1,7 @@
 // C ABI of the library (include/nvpt2.h): context handling, argument checks,
 // host<->device staging for the drop-in host-pointer entry points, and the
 // device-pointer (_d) entry points that enqueue the kernels.
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -502,6 +503,35 @@ int nvpt_dgemm_split_d(nvpt_context *ctx, int64_t m, int64_t n, int64_t k, const
     if (rc2 == 4) return fail(ctx, NVPT_ETIMEDOUT, "dgemm_split: the product timed out waiting on its pipeline");
     if (rc2) return fail(ctx, NVPT_ECUDA, "dgemm_split: error flag read-back failed");
     return after_launch(ctx, "dgemm_split");
+}
+
+int nvpt_dgemm_split_ex_d(nvpt_context *ctx, int transa, int transb, int64_t m, int64_t n, int64_t k, double alpha,
+                          const double *A, int64_t lda, const double *B, int64_t ldb, double beta, double *C,
+                          int64_t ldc, void *stream) {
+    if (!ctx || !A || !B || !C) return NVPT_EINVAL;
+    int e2 = 0;
+    if (m < 1 || n < 1 || k < 1 || k > oz::kWideMaxK || ldc < n || lda < (transa ? m : k) ||
+        ldb < (transb ? k : n) || std::frexp(std::fabs(alpha), &e2) != 0.5)
+        return fail(ctx, NVPT_EINVAL,
+                    "dgemm_split_ex: need m, n >= 1, 1 <= k <= 2^19, lda/ldb/ldc >= the row lengths, alpha = +-2^e");
+    cudaStream_t st = pick(ctx, stream);
+    oz::WideGemm g;
+    g.m = m; g.n = n; g.K = (int)k;
+    g.A = A; g.a_r = transa ? 1 : lda; g.a_k = transa ? lda : 1;
+    g.B = B; g.b_c = transb ? ldb : 1; g.b_k = transb ? 1 : ldb;
+    g.alpha = alpha; g.beta = beta; g.C = C; g.ldc = ldc;
+    const size_t bytes = oz::oz_wide_bytes(m, n, (int)k) + 256;
+    void *w = nullptr;
+    NV_TRY(cuda_check(ctx, cudaMallocAsync(&w, bytes, st), "dgemm_split_ex workspace"));
+    int *err = (int *)((uint8_t *)w + bytes - 256);
+    cudaMemsetAsync(err, 0, sizeof(int), st);
+    int rc = oz::oz_gemm_wide(g, w, err, st);
+    int rc2 = rc ? 0 : oz::oz_check_error(err, st);
+    cudaFreeAsync(w, st);
+    if (rc) return fail(ctx, NVPT_ECUDA, "dgemm_split_ex: launch failed");
+    if (rc2 == 4) return fail(ctx, NVPT_ETIMEDOUT, "dgemm_split_ex: the product timed out waiting on its pipeline");
+    if (rc2) return fail(ctx, NVPT_ECUDA, "dgemm_split_ex: error flag read-back failed");
+    return after_launch(ctx, "dgemm_split_ex");
 }
 
 int nvpt_bbmat_d(nvpt_context *ctx, const double *atwo, double *bmat, double *btmat, const double *daaa,

@@ -72,5 +72,29 @@ int oz_gemm_skinny(const OzPlan &pl, const double *const *X, const double *const
                    int ldt, void *work, cudaStream_t st);
 int oz_check_error(const void *work, cudaStream_t st);
 
+// General products (ozaki_wide.cu): C[m, n] (row-major, ldc) =
+// alpha X Y + beta C for FP64 operands of any shape, X[i, k] =
+// A[i * a_r + k * a_k] (i < m, k < K), Y[k, j] = B[j * b_c + k * b_k].
+// alpha must be a power of two times +-1 (it is folded into the column
+// exponents).  lower: only the output tiles that meet the lower triangle
+// (j <= i) are formed (symmetric products; the caller mirrors).
+struct WideGemm {
+    long long m = 0, n = 0;
+    int K = 0;
+    const double *A = nullptr;
+    long long a_r = 0, a_k = 0;
+    const double *B = nullptr;
+    long long b_c = 0, b_k = 0;
+    double alpha = 1.0, beta = 0.0;
+    double *C = nullptr;
+    long long ldc = 0;
+    bool lower = false;
+};
+constexpr int kWideMaxK = 1 << 19;  // keeps the 64-bit drain sums in range
+size_t oz_wide_bytes(long long m, long long n, int K);  // device workspace (16-byte aligned)
+// Enqueue on `st`; 0 on success, 1 bad arguments, 3 launch failure.  A wait
+// that timed out sets the int at err (device memory, not reset here).
+int oz_gemm_wide(const WideGemm &g, void *work, int *err, cudaStream_t st);
+
 }  // namespace oz
 }  // namespace nvpt

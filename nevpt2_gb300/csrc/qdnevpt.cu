@@ -151,6 +151,68 @@ __global__ void k_pc_finish(const double *R, const double *Rp, const double *Rj,
     for (int j = 0; j < nother && j < 8; ++j) block_add(offs[j], acc + 2 + j);
 }
 
+// PC sums of one class from the tridiagonal form of its pencil: for label l
+// (one thread each) with shift sig[l], x = (T + sig I)^-1 y_l by Gaussian
+// elimination with partial pivoting on the tridiagonal T (d[n], e[n-1]),
+// then
+//   acc[0] -= y_l . x,   acc[1] += x . x,   acc[2 + k] -= y_{k+1,l} . x,
+// which are the type-0 sums of k_pc_finish over the eigenpairs of T
+// (sum_mu r_mu^2 / (w_mu + sig) = y^T (T + sig)^-1 y with r = G^T y).
+// Y is row-major [n][ncol], column k L + l holding block k (0: own state,
+// k > 0: the other states) of label l.  Work arrays are [n][L] (label
+// fastest, so that the threads' accesses coalesce).
+__global__ void k_tridiag_resolvent(const double *d, const double *e, long long n, const double *Y, long long ncol,
+                                    long long L, int nother, const double *sig, double *wb, double *wc, double *wd,
+                                    double *wy, double *acc) {
+    const long long l = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double en = 0.0, ps = 0.0;
+    double offs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (l < L && n > 0) {
+        const double s = sig[l];
+        auto at = [&](long long i) { return i * L + l; };
+        // row i: diagonal b, super-diagonal c, second super-diagonal (fill) dd
+        double b = d[0] + s, cc = n > 1 ? e[0] : 0.0, y = Y[l];
+        for (long long i = 0; i + 1 < n; ++i) {
+            const double a1 = e[i];                          // row i+1, column i
+            const double b1 = d[i + 1] + s;                  // row i+1, column i+1
+            const double c1 = i + 2 < n ? e[i + 1] : 0.0;    // row i+1, column i+2
+            const double y1 = Y[(i + 1) * ncol + l];
+            if (fabs(b) >= fabs(a1)) {  // keep row i as pivot row
+                const double f = a1 / b;
+                wb[at(i)] = b; wc[at(i)] = cc; wd[at(i)] = 0.0; wy[at(i)] = y;
+                b = b1 - f * cc;
+                cc = c1;
+                y = y1 - f * y;
+            } else {                    // interchange rows i and i+1
+                const double f = b / a1;
+                wb[at(i)] = a1; wc[at(i)] = b1; wd[at(i)] = c1; wy[at(i)] = y1;
+                b = cc - f * b1;
+                cc = -f * c1;
+                y = y - f * y1;
+            }
+        }
+        wb[at(n - 1)] = b; wy[at(n - 1)] = y;
+        // back substitution, x over wy
+        double x2 = 0.0, x1 = y / b;
+        wy[at(n - 1)] = x1;
+        for (long long i = n - 2; i >= 0; --i) {
+            const double x = (wy[at(i)] - wc[at(i)] * x1 - wd[at(i)] * x2) / wb[at(i)];
+            wy[at(i)] = x;
+            x2 = x1;
+            x1 = x;
+        }
+        for (long long i = 0; i < n; ++i) {
+            const double x = wy[at(i)];
+            en -= Y[i * ncol + l] * x;
+            ps += x * x;
+            for (int k = 0; k < nother && k < 8; ++k) offs[k] -= Y[i * ncol + (k + 1) * L + l] * x;
+        }
+    }
+    block_add(en, acc + 0);
+    block_add(ps, acc + 1);
+    for (int j = 0; j < nother && j < 8; ++j) block_add(offs[j], acc + 2 + j);
+}
+
 // v0 (class 0): labels (ii <= ij) x (r <= s); G[i,r,j,s] = (i r | j s) wait: G = Rcv^T Rcv
 __global__ void k_v0(const double *G, const double *eps, int nc, int nv, int voff, const unsigned char *fro,
                      double *acc) {
@@ -610,6 +672,21 @@ class Runner {
         if (L * nmu > 0) {
             k_pc_finish<<<nblk(L * nmu), TPB, 0, c.st>>>(R.p, Rp ? Rp->p : nullptr, Rj.p, Rpj ? Rpj->p : nullptr,
                                                           M - 1, w.p, bs.p, L, nmu, type, a.p);
+            LAUNCHED();
+        }
+        return download(c, a.p, 2 + 8);
+    }
+    // PC sums from the tridiagonal form of a pencil: Yt row-major [n][M L]
+    // (column k L + l: state block k of label l), shifts per label.
+    std::vector<double> resolvent_sums(const PencilTridiag &PT, const T &Yt, const std::vector<double> &shift) {
+        const long long L = (long long)shift.size(), n = PT.n;
+        T sg = upload(c, shift);
+        T a = alloc(c, {2 + 8}, true);
+        if (L > 0 && n > 0) {
+            T wb = alloc(c, {n, L}, false), wc = alloc(c, {n, L}, false), wd = alloc(c, {n, L}, false),
+              wy = alloc(c, {n, L}, false);
+            k_tridiag_resolvent<<<(unsigned)((L + 63) / 64), 64, 0, c.st>>>(PT.d.p, PT.e.p, n, Yt.p, Yt.sh[1], L, M - 1,
+                                                                            sg.p, wb.p, wc.p, wd.p, wy.p, a.p);
             LAUNCHED();
         }
         return download(c, a.p, 2 + 8);
@@ -1320,21 +1397,16 @@ class Runner {
         T K = permuted(c, A, {3, 4, 5, 0, 1, 2});
         S = view2(std::move(S), n3, n3);
         K = view2(std::move(K), n3, n3);
-        PcResult P = pc_transform(c, S, K, n3, thr);
-        acc.nnew[(minus ? 7 : 6) + 10 * s] = P.nnew;
         T W2t = permuted(c, W2, {3, 0, 1, 2});                 // [a, (ap,bp,cp)]
         W2t = view2(std::move(W2t), n, n3);
-        // R[l, mu] = sum_x (Vd S + H W2t)[l, x] C[x, mu]: the order-n3 products
-        // S C and W2t C of the reference are reassociated onto the L rows.
-        auto rm = [&](const T &S_, const T &W2_, double *out) {
-            T Z = alloc(c, {L, (long long)n3}, false);
-            gemm(c, false, false, L, n3, n3, 1.0, Vd.p, n3, S_.p, n3, 0.0, Z.p, n3);
-            gemm(c, false, false, L, n3, n, 1.0, H.p, n, W2_.p, n3, 1.0, Z.p, n3);
-            gemm(c, false, false, L, n3, n3, 1.0, Z.p, n3, P.C.p, n3, 0.0, out, n3);
+        // Z[l, x] = (Vd S + H W2t)[l, x]: the numerators of the reference
+        // before the change to the PC basis (R = Z C).
+        auto zm = [&](const T &S_, const T &W2_, double *out) {
+            gemm(c, false, false, L, n3, n3, 1.0, Vd.p, n3, S_.p, n3, 0.0, out, n3);
+            gemm(c, false, false, L, n3, n, 1.0, H.p, n, W2_.p, n3, 1.0, out, n3);
         };
-        T R = alloc(c, {L, (long long)n3}, false);
-        rm(S, W2t, R.p);
-        T Rj = stack_others(L, n3, [&](int j, double *out) {
+        // the same rows with the transition metric of another state j
+        auto other_z = [&](int j, double *out) {
             auto [PD, lt] = off(j);
             T E2o = alloc(c, {n, n, n, n}, false), E3o = alloc(c, {n, n, n, n, n, n}, false);
             build_ee2L(c, PD->d2.p, PD->d1.p, n, E2o.p);
@@ -1368,13 +1440,41 @@ class Runner {
             So = view2(std::move(So), n3, n3);
             T W2ot = permuted(c, W2o, {3, 0, 1, 2});
             W2ot = view2(std::move(W2ot), n, n3);
-            rm(So, W2ot, out);
-        });
+            zm(So, W2ot, out);
+        };
         std::vector<double> pb(L);  // deno = w + eps_r  /  w - eps_i
         for (long long l = 0; l < L; ++l) pb[l] = -base[l];
         std::vector<double> e2(M * M, 0.0);
         double psi2 = 0.0;
-        pc_accum(e2, psi2, pc_finish(R, nullptr, Rj, nullptr, P.w, pb, n3, 0));
+        PencilTridiag PT;
+        if (n3 >= kPcCholMin && metric_above(c, S.p, n3, thr) && pencil_tridiag(c, K.p, S.p, n3, PT)) {
+            // Every metric eigenvalue is kept (nnew = n3): the PC sums over
+            // the eigenpairs of K v = w S v are resolvents of the pencil,
+            //   sum_mu r_mu^2 / (w_mu + s) = z^T (K + s S)^-1 z,
+            // evaluated in the pencil's tridiagonal form (no eigenvectors).
+            acc.nnew[(minus ? 7 : 6) + 10 * s] = (int)n3;
+            T Z = alloc(c, {(long long)M, L, (long long)n3}, false);  // own state, then the others
+            zm(S, W2t, Z.p);
+            auto o = others();
+            for (size_t k = 0; k < o.size(); ++k) other_z(o[k], Z.p + (long long)(k + 1) * L * n3);
+            pencil_rhs(c, PT, Z.p, (long long)M * L);  // rows of Z are the columns of a column-major [n3, M L]
+            Z = view2(std::move(Z), (long long)M * L, n3);
+            T Yt = permuted(c, Z, {1, 0});  // [n3][M L]
+            pc_accum(e2, psi2, resolvent_sums(PT, Yt, pb));
+        } else {
+            PcResult P = pc_transform(c, S, K, n3, thr);
+            acc.nnew[(minus ? 7 : 6) + 10 * s] = P.nnew;
+            // R[l, mu] = sum_x Z[l, x] C[x, mu]: the order-n3 products S C and
+            // W2t C of the reference are reassociated onto the L rows.
+            T Z = alloc(c, {L, (long long)n3}, false), R = alloc(c, {L, (long long)n3}, false);
+            zm(S, W2t, Z.p);
+            gemm(c, false, false, L, n3, n3, 1.0, Z.p, n3, P.C.p, n3, 0.0, R.p, n3);
+            T Rj = stack_others(L, n3, [&](int j, double *out) {
+                other_z(j, Z.p);
+                gemm(c, false, false, L, n3, n3, 1.0, Z.p, n3, P.C.p, n3, 0.0, out, n3);
+            });
+            pc_accum(e2, psi2, pc_finish(R, nullptr, Rj, nullptr, P.w, pb, n3, 0));
+        }
         pc_store(minus ? 6 : 5, e2, psi2, true);
     }
 };  // class Runner
@@ -1471,6 +1571,10 @@ struct ClassStreams {
             if (done[k]) cudaEventDestroy(done[k]);
         }
         if (prep) cudaEventDestroy(prep);
+        for (auto &x : c) {
+            x.split = false;
+            x.oz_err = nullptr;
+        }
         CtxPool::release(c, dev);
     }
 };
@@ -1500,6 +1604,13 @@ int run_qdnevpt(nvpt_context *ctx, cudaStream_t st, const nvpt_qdnevpt_in *in, n
             cusolverDnDestroy(c.sol);
         }
     } guard{c};
+    // split precision: the stage's large products run as Ozaki digit products
+    c.split = nvpt_get_precision(ctx) == NVPT_PRECISION_SPLIT;
+    T ozerr;
+    if (c.split) {
+        ozerr = alloc(c, {1}, true);
+        c.oz_err = (int *)ozerr.p;
+    }
     int n = na;
     long long n2 = (long long)n * n, n4 = n2 * n2, n6 = n4 * n2;
     long long npair = (long long)norb * (norb + 1) / 2;
@@ -1594,6 +1705,11 @@ int run_qdnevpt(nvpt_context *ctx, cudaStream_t st, const nvpt_qdnevpt_in *in, n
     int dev = 0;
     ck(cudaGetDevice(&dev), "cudaGetDevice");
     ClassStreams ps((size_t)M), cs((size_t)M * nj);
+    for (auto *pool : {&ps, &cs})
+        for (auto &pc_ : pool->c) {
+            pc_.split = c.split;
+            pc_.oz_err = c.oz_err;
+        }
     ck(cudaEventRecord(ps.prep, c.st), "event");  // B and h ready
     std::vector<std::unique_ptr<Runner>> SR(M);
     {
@@ -1655,6 +1771,14 @@ int run_qdnevpt(nvpt_context *ctx, cudaStream_t st, const nvpt_qdnevpt_in *in, n
     }
     SR.clear();
     ck(cudaStreamSynchronize(c.st), "qdnevpt sync");
+    if (c.split) {
+        int h = 0;
+        ck(cudaMemcpy(&h, c.oz_err, sizeof(int), cudaMemcpyDeviceToHost), "error flag");
+        if (h) {
+            err = "qdnevpt: a split-precision product timed out waiting on its pipeline";
+            return NVPT_ETIMEDOUT;
+        }
+    }
     auto put = [](double *dst, const std::vector<double> &v) {
         if (dst) std::memcpy(dst, v.data(), sizeof(double) * v.size());
     };

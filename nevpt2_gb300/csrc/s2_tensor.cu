@@ -1,6 +1,11 @@
 // Implementation of the device tensor toolkit (see s2_tensor.cuh).
 #include "s2_tensor.cuh"
 
+#include <algorithm>
+#include <cmath>
+
+#include "ozaki.cuh"
+
 namespace nvpt {
 namespace s2 {
 
@@ -204,9 +209,35 @@ T permuted(Ctx &c, const T &in, const std::vector<int> &axes, double alpha) {
     return out;
 }
 
+namespace {
+// Products big enough to pay for the digit splits; alpha = +-2^e.
+bool split_product(const Ctx &c, long long m, long long n, long long k, double alpha) {
+    if (!c.split || k < 64 || k > oz::kWideMaxK || m < 64 || n < 16) return false;
+    if ((double)m * (double)n * (double)k < 6.7e7) return false;
+    int e = 0;
+    return std::frexp(std::fabs(alpha), &e) == 0.5;
+}
+void split_gemm(Ctx &c, const oz::WideGemm &g) {
+    void *w = nullptr;
+    ck(cudaMallocAsync(&w, oz::oz_wide_bytes(g.m, g.n, g.K), c.st), "cudaMallocAsync");
+    const int rc = oz::oz_gemm_wide(g, w, c.oz_err, c.st);
+    cudaFreeAsync(w, c.st);
+    if (rc) throw Error(2, "split-precision product failed to launch");
+}
+}  // namespace
+
 void gemm(Ctx &c, bool ta, bool tb, long long m, long long n, long long k, double alpha, const double *A, long long lda,
           const double *B, long long ldb, double beta, double *C, long long ldc) {
     if (m == 0 || n == 0) return;
+    if (split_product(c, m, n, k, alpha)) {
+        oz::WideGemm g;
+        g.m = m; g.n = n; g.K = (int)k;
+        g.A = A; g.a_r = ta ? 1 : lda; g.a_k = ta ? lda : 1;
+        g.B = B; g.b_c = tb ? ldb : 1; g.b_k = tb ? 1 : ldb;
+        g.alpha = alpha; g.beta = beta; g.C = C; g.ldc = ldc;
+        split_gemm(c, g);
+        return;
+    }
     // Row-major C = op(A) op(B)  <=>  column-major C^T = op(B)^T op(A)^T.
     ck(cublasDgemm(c.blas, tb ? CUBLAS_OP_T : CUBLAS_OP_N, ta ? CUBLAS_OP_T : CUBLAS_OP_N, (int)n, (int)m, (int)k,
                    &alpha, B, (int)ldb, A, (int)lda, &beta, C, (int)ldc),
@@ -267,6 +298,18 @@ __global__ void k_mirror_lower(double *o, long long m) {
 
 void gram(Ctx &c, const double *X, long long Q, long long m, double *out) {
     if (m == 0) return;
+    if (split_product(c, m, m, Q, 1.0)) {
+        // the tiles meeting the lower triangle of out = X^T X, then mirrored
+        oz::WideGemm g;
+        g.m = m; g.n = m; g.K = (int)Q;
+        g.A = X; g.a_r = 1; g.a_k = m;
+        g.B = X; g.b_c = 1; g.b_k = m;
+        g.C = out; g.ldc = m; g.lower = true;
+        split_gemm(c, g);
+        k_mirror_lower<<<nblk(m * m), TPB, 0, c.st>>>(out, m);
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+        return;
+    }
     const double one = 1.0, zero = 0.0;
     // column-major view: X is m x Q (ld m); C = X X^T fills the column-major
     // upper triangle = the row-major lower triangle of out
@@ -321,6 +364,131 @@ bool sygvd_upper(Ctx &c, const double *K, const double *S, long long n, double *
     cudaFreeAsync(info, c.st);
     cudaFreeAsync(B, c.st);
     return hinfo == 0;
+}
+
+namespace {
+// cuSOLVER workspace of `count` doubles + info word, stream-ordered.
+struct SolverWork {
+    Ctx &c;
+    double *w = nullptr;
+    int *info = nullptr;
+    SolverWork(Ctx &cc, int count) : c(cc) {
+        ck(cudaMallocAsync((void **)&w, sizeof(double) * (size_t)(count > 0 ? count : 1), c.st), "cudaMallocAsync");
+        ck(cudaMallocAsync((void **)&info, sizeof(int), c.st), "cudaMallocAsync");
+    }
+    int status() {
+        int h = -1;
+        ck(cudaMemcpyAsync(&h, info, sizeof(int), cudaMemcpyDeviceToHost, c.st), "info copy");
+        ck(cudaStreamSynchronize(c.st), "solver sync");
+        return h;
+    }
+    ~SolverWork() {
+        cudaFreeAsync(w, c.st);
+        cudaFreeAsync(info, c.st);
+    }
+};
+}  // namespace
+
+namespace {
+// Mirror the upper triangle of the kb x kb diagonal block at A (column-major,
+// ld) into its lower triangle.
+__global__ void k_mirror_block(double *A, long long ld, int kb) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)kb * kb) return;
+    const int i = (int)(t % kb), j = (int)(t / kb);
+    if (i > j) A[i + j * ld] = A[j + i * ld];
+}
+}  // namespace
+
+// Upper triangle of A (column-major n x n, symmetric on entry) <- the upper
+// triangle of U^-T A U^-1, U upper triangular: the blocked right-looking
+// reduction of a symmetric-definite pencil to standard form (n^3 flops, half
+// of two full triangular solves).  Per diagonal block k of width kb, with the
+// trailing blocks 12 (kb x m) and 22:
+//   A11 <- U11^-T A11 U11^-1
+//   A12 <- U11^-T A12 - 1/2 A11 U12
+//   A22 <- A22 - A12^T U12 - U12^T A12          (upper triangle)
+//   A12 <- (A12 - 1/2 A11 U12) U22^-1
+// after which A22 is reduced in turn.  The lower triangle is left stale.
+void reduce_to_standard(Ctx &c, double *A, const double *U, long long n) {
+    constexpr int NB = 256;
+    const double one = 1.0, mhalf = -0.5, mone = -1.0;
+    for (long long k = 0; k < n; k += NB) {
+        const int kb = (int)std::min<long long>(NB, n - k), m = (int)(n - k - kb);
+        double *A11 = A + k + k * n;
+        const double *U11 = U + k + k * n;
+        k_mirror_block<<<nblk((long long)kb * kb), TPB, 0, c.st>>>(A11, n, kb);
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+        ck(cublasDtrsm(c.blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, kb, kb,
+                       &one, U11, (int)n, A11, (int)n),
+           "trsm");
+        ck(cublasDtrsm(c.blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, kb, kb,
+                       &one, U11, (int)n, A11, (int)n),
+           "trsm");
+        if (m == 0) break;
+        double *A12 = A + k + (k + kb) * n, *A22 = A + (k + kb) + (k + kb) * n;
+        const double *U12 = U + k + (k + kb) * n, *U22 = U + (k + kb) + (k + kb) * n;
+        ck(cublasDtrsm(c.blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, kb, m,
+                       &one, U11, (int)n, A12, (int)n),
+           "trsm");
+        ck(cublasDsymm(c.blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, kb, m, &mhalf, A11, (int)n, U12, (int)n, &one,
+                       A12, (int)n),
+           "symm");
+        ck(cublasDsyr2k(c.blas, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, m, kb, &mone, A12, (int)n, U12, (int)n, &one, A22,
+                        (int)n),
+           "syr2k");
+        ck(cublasDsymm(c.blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, kb, m, &mhalf, A11, (int)n, U12, (int)n, &one,
+                       A12, (int)n),
+           "symm");
+        ck(cublasDtrsm(c.blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, kb, m,
+                       &one, U22, (int)n, A12, (int)n),
+           "trsm");
+    }
+}
+
+bool pencil_tridiag(Ctx &c, const double *K, const double *S, long long n, PencilTridiag &P) {
+    P.n = n;
+    if (n == 0) return true;
+    const int N = (int)n;
+    P.U = alloc(c, {n, n}, false);
+    P.A = alloc(c, {n, n}, false);
+    P.d = alloc(c, {n}, false);
+    P.e = alloc(c, {n}, true);
+    P.tau = alloc(c, {n}, true);
+    symmetrize_upper(c, S, n, P.U.p);
+    symmetrize_upper(c, K, n, P.A.p);
+    int lw_p = 0, lw_t = 0;
+    ck(cusolverDnDpotrf_bufferSize(c.sol, CUBLAS_FILL_MODE_UPPER, N, P.U.p, N, &lw_p), "potrf_bufferSize");
+    ck(cusolverDnDsytrd_bufferSize(c.sol, CUBLAS_FILL_MODE_UPPER, N, P.A.p, N, P.d.p, P.e.p, P.tau.p, &lw_t),
+       "sytrd_bufferSize");
+    SolverWork sw(c, lw_p > lw_t ? lw_p : lw_t);
+    ck(cusolverDnDpotrf(c.sol, CUBLAS_FILL_MODE_UPPER, N, P.U.p, N, sw.w, lw_p, sw.info), "potrf");
+    if (sw.status() != 0) return false;
+    reduce_to_standard(c, P.A.p, P.U.p, n);
+    ck(cusolverDnDsytrd(c.sol, CUBLAS_FILL_MODE_UPPER, N, P.A.p, N, P.d.p, P.e.p, P.tau.p, sw.w, lw_t, sw.info),
+       "sytrd");
+    const int st = sw.status();
+    if (st != 0) throw Error(2, "sytrd failed, info=" + std::to_string(st));
+    return true;
+}
+
+void pencil_rhs(Ctx &c, const PencilTridiag &P, double *Y, long long m) {
+    if (P.n == 0 || m == 0) return;
+    const int N = (int)P.n, Mc = (int)m;
+    const double one = 1.0;
+    ck(cublasDtrsm(c.blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, N, Mc, &one,
+                   P.U.p, N, Y, N),
+       "trsm");
+    int lw = 0;
+    ck(cusolverDnDormtr_bufferSize(c.sol, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, N, Mc, P.A.p, N,
+                                   P.tau.p, Y, N, &lw),
+       "ormtr_bufferSize");
+    SolverWork sw(c, lw);
+    ck(cusolverDnDormtr(c.sol, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, N, Mc, P.A.p, N, P.tau.p, Y, N,
+                        sw.w, lw, sw.info),
+       "ormtr");
+    const int st = sw.status();
+    if (st != 0) throw Error(2, "ormtr failed, info=" + std::to_string(st));
 }
 
 void build_ee2L(Ctx &c, const double *taa, const double *dal, int n, double *out) {

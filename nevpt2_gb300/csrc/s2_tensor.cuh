@@ -76,6 +76,10 @@ struct Ctx {
     cudaStream_t st;
     cublasHandle_t blas;
     cusolverDnHandle_t sol;
+    // Split precision: large GEMMs (and Gram matrices) run as Ozaki digit
+    // products on the tensor cores; a pipeline timeout sets *oz_err.
+    bool split = false;
+    int *oz_err = nullptr;
 };
 
 T alloc(Ctx &c, std::initializer_list<long long> shape, bool zero = true);
@@ -116,6 +120,23 @@ bool metric_above(Ctx &c, const double *A, long long n, double thr);
 bool sygvd_upper(Ctx &c, const double *K, const double *S, long long n, double *w, double *V);
 // Symmetric copy: out = triu(A) + triu(A,1)^T.
 void symmetrize_upper(Ctx &c, const double *A, long long n, double *out);
+
+// The pencil K v = w S v in tridiagonal form, without its eigenvectors:
+// S = U^T U (Cholesky of the symmetric view of S), K~ = U^-T K U^-1 (K's
+// symmetric view), K~ = Q T Q^T (Householder).  T: diagonal d[n],
+// off-diagonal e[n-1].  U, Q (reflectors + tau) stay in the struct, which
+// then maps right-hand sides into T's basis.  False if S is not positive
+// definite.
+struct PencilTridiag {
+    T U, A, d, e, tau;  // U: column-major upper factor; A: reflectors of Q
+    long long n = 0;
+};
+bool pencil_tridiag(Ctx &c, const double *K, const double *S, long long n, PencilTridiag &P);
+// Upper triangle of A (column-major, symmetric) <- that of U^-T A U^-1.
+void reduce_to_standard(Ctx &c, double *A, const double *U, long long n);
+// Y <- Q^T U^-T Y for Y column-major [n, m] (= row-major [m, n]): each row
+// z of the row-major view becomes y with z^T (K + s S)^-1 z = y^T (T + s)^-1 y.
+void pencil_rhs(Ctx &c, const PencilTridiag &P, double *Y, long long m);
 
 // Accessor builders (C-ordered n-index tensors of one state or pair).
 void build_ee2L(Ctx &c, const double *taa, const double *dal, int n, double *out);

@@ -105,3 +105,76 @@ def test_split_energies_within_1e7_of_fp64():
     assert abs(esp.e2mp[0, 0] - e64.e2mp[0, 0]) <= 1e-7
     assert abs(esp.e2en[0, 0] - e64.e2en[0, 0]) <= 1e-7
     assert np.array_equal(esp.nnew, e64.nnew)
+
+
+# ---------------------------------------------------------------- general products
+def _split_ex(A, B, ta=False, tb=False, alpha=1.0, beta=0.0, C0=None):
+    """Row-major C = alpha op(A) op(B) + beta C0 through nvpt_dgemm_split_ex_d."""
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda:0")
+    m = A.shape[1] if ta else A.shape[0]
+    k = A.shape[0] if ta else A.shape[1]
+    n = B.shape[0] if tb else B.shape[1]
+    tA = torch.from_numpy(np.ascontiguousarray(A)).to(dev)
+    tB = torch.from_numpy(np.ascontiguousarray(B)).to(dev)
+    tC = (torch.from_numpy(np.ascontiguousarray(C0)).to(dev) if C0 is not None
+          else torch.full((m, n), float("nan"), dtype=torch.float64, device=dev))
+    ctx = koopro.context()
+    ctx.call("nvpt_dgemm_split_ex_d", int(ta), int(tb), m, n, k, alpha, ptr(tA), A.shape[1], ptr(tB), B.shape[1],
+             beta, ptr(tC), n, None)
+    ctx.synchronize()
+    return tC.cpu().numpy()
+
+
+def _bound_ex(X, Y):
+    """Per-term error 2^-59 max|X_i| max|Y_j| plus the FP64 reference's own rounding."""
+    k = X.shape[1]
+    split = k * 2.0**-59 * np.abs(X).max(axis=1)[:, None] * np.abs(Y).max(axis=0)[None, :]
+    return split + k * 2.0**-53 * (np.abs(X) @ np.abs(Y))
+
+
+@pytest.mark.parametrize("m,n,k,ta,tb", [(128, 32, 64, False, False), (300, 77, 1184, False, False),
+                                         (257, 500, 100, True, False), (1000, 1000, 4096, False, True),
+                                         (33, 5, 3000, True, True), (7, 1, 1, False, False),
+                                         (640, 96, 1537, False, False)])
+def test_split_ex_within_bound(m, n, k, ta, tb):
+    rng = np.random.default_rng(m + 3 * n + 7 * k)
+    A = rng.standard_normal((k, m) if ta else (m, k))
+    B = rng.standard_normal((n, k) if tb else (k, n)) * 0.05
+    X = A.T if ta else A
+    Y = B.T if tb else B
+    C = _split_ex(A, B, ta, tb)
+    ref = X @ Y
+    assert np.isfinite(C).all()
+    err = np.abs(C - ref)
+    assert (err <= _bound_ex(X, Y)).all()
+    assert err.max() <= 1e-14 * np.abs(ref).max()
+
+
+def test_split_ex_exact_on_small_integers():
+    rng = np.random.default_rng(15)
+    A = rng.integers(-63, 64, (256, 2000)).astype(np.float64)
+    B = rng.integers(-63, 64, (2000, 96)).astype(np.float64)
+    assert np.array_equal(_split_ex(A, B), A @ B)
+
+
+def test_split_ex_alpha_beta_scales_and_zero_rows():
+    rng = np.random.default_rng(16)
+    A = rng.standard_normal((384, 700)) * (10.0 ** rng.uniform(-8, 3, 384))[:, None]
+    A[17] = 0.0
+    B = rng.standard_normal((700, 200)) * (10.0 ** rng.uniform(-4, 4, 200))[None, :]
+    C0 = rng.standard_normal((384, 200))
+    C = _split_ex(A, B, alpha=-0.5, beta=1.0, C0=C0)
+    ref = -0.5 * (A @ B) + C0
+    assert (np.abs(C - ref) <= 0.5 * _bound_ex(A, B) + 2.0**-52 * np.abs(ref)).all()
+    assert np.array_equal(C[17], C0[17])
+
+
+def test_split_ex_rejects_bad_arguments():
+    ctx = koopro.context()
+    x = np.zeros(1)
+    with pytest.raises(NvptError) as e:
+        ctx.call("nvpt_dgemm_split_ex_d", 0, 0, 4, 4, 4, 3.0, ptr(x), 4, ptr(x), 4, 0.0, ptr(x), 4, None)
+    assert e.value.status == 1
+    with pytest.raises(NvptError):
+        ctx.call("nvpt_dgemm_split_ex_d", 0, 0, 4, 4, 4, 1.0, ptr(x), 3, ptr(x), 4, 0.0, ptr(x), 4, None)
