@@ -451,6 +451,26 @@ def run_ours(args):
     bamat_sp_ms = bamat_alone()
     oz_ms, oz_n, oz_bytes = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
     ctx.call("nvpt_profile_read", b"oz_gemm", ctypes.byref(oz_ms), ctypes.byref(oz_n), ctypes.byref(oz_bytes))
+    # the general split product alone, at the shape of the stage's largest
+    # integral blocks ((i r | j s): nc nv x nc nv x Q), CUDA events per launch
+    mw, nw_, kw = p.ncore * p.nvirt, p.ncore * p.nvirt, p.chol.shape[0]
+    gw = torch.Generator(device=dev)
+    gw.manual_seed(5)
+    Aw = torch.randn((kw, mw), dtype=torch.float64, device=dev, generator=gw)
+    Cw = torch.empty((mw, nw_), dtype=torch.float64, device=dev)
+    for _ in range(2):  # warm
+        ctx.call("nvpt_dgemm_split_ex_d", 1, 0, mw, nw_, kw, 1.0, ptr(Aw), mw, ptr(Aw), mw, 0.0, ptr(Cw), nw_,
+                 ptr_stream(stream))
+    torch.cuda.synchronize(dev)
+    ctx.call("nvpt_set_profiling", 1)
+    for _ in range(3):
+        flush.zero_()
+        ctx.call("nvpt_dgemm_split_ex_d", 1, 0, mw, nw_, kw, 1.0, ptr(Aw), mw, ptr(Aw), mw, 0.0, ptr(Cw), nw_,
+                 ptr_stream(stream))
+    torch.cuda.synchronize(dev)
+    ow_ms, ow_n, ow_fl = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
+    ctx.call("nvpt_profile_read", b"oz_wide", ctypes.byref(ow_ms), ctypes.byref(ow_n), ctypes.byref(ow_fl))
+    del Aw, Cw
     ctx.call("nvpt_set_profiling", 0)
     set_mode(koopro.FP64)
 
@@ -505,6 +525,10 @@ def run_ours(args):
     pk = _peaks()
     hbm_peak = pk.get("hbm_gbs", 6800.0)
     oz_gbs = oz_bytes.value / (oz_ms.value * 1e-3) / 1e9 if oz_ms.value > 0 else None
+    # roofline (split stage 2): the general product runs 64 BF16 digit
+    # products per FP64-equivalent product; tensor-bound
+    bf16_peak = pk.get("bf16_tflops", 1900.0)
+    ow_tf = 64 * ow_fl.value / (ow_ms.value * 1e-3) / 1e12 if ow_ms.value > 0 else None
     de = lambda a_, b_: float(np.abs(np.asarray(a_) - np.asarray(b_)).max())
     koop = {k: st.result(k) for k in st.out}
     koop.update({"1-RDM": p.dal, "2-RDM": p.taa, "3-RDM": p.daaa})
@@ -514,7 +538,7 @@ def run_ours(args):
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded CI vector, exact RDMs, random DF integrals)",
             "config": workload_desc(p), "gpu_launches": int(launches),
             "e2e": {"value": e2e, "unit": "s/state", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-            "roofline": {"kernel": "bamat (k_bamat_slabs + cuBLAS DGEMM + k_rest_*)", "bound": "tensor",
+            "roofline": {"kernel": "bamat (k_bamat_slabs_t + cuBLAS DGEMM + k_rest_*)", "bound": "tensor",
                          "achieved": achieved, "peak": peak64, "unit": "TFLOP/s", "frac": achieved / peak64,
                          "traffic": None, "precision": "fp64",
                          "peak_source": "FP64 DGEMM rate measured live in this run (cuBLAS 4096^3)",
@@ -533,6 +557,14 @@ def run_ours(args):
                                    "frac": (oz_gbs / hbm_peak) if oz_gbs else None, "traffic": None,
                                    "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
                                    "kernel_ms": oz_ms.value, "launches": oz_n.value, "alg_bytes": oz_bytes.value},
+                      "roofline_stage2": {
+                          "kernel": "k_oz_wide (general Ozaki digit products, tcgen05), alone at the (i r|j s) shape",
+                          "shape": [mw, nw_, kw], "bound": "tensor", "achieved": ow_tf, "peak": bf16_peak,
+                          "unit": "TFLOP/s (BF16 digit products)",
+                          "frac": (ow_tf / bf16_peak) if ow_tf else None, "traffic": None,
+                          "peak_source": "MEASURED_PEAKS.json bf16_tflops (of measured, burst)",
+                          "fp64_equivalent_tflops": (ow_tf / 64) if ow_tf else None,
+                          "kernel_ms": (ow_ms.value / ow_n.value) if ow_n.value else None},
                       "clocks": clk_sp, "step_ms_all": times_sp},
             "stage2_ms_per_piece": s2_breakdown,
             "energies": energy_summary(energies),

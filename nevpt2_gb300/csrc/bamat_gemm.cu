@@ -61,6 +61,80 @@ __global__ void __launch_bounds__(256) k_bamat_slabs(Rdm r, int s, const int *sl
     X4[base + (((ll)v * n + w) * n + z) * n3 + ((ll)u * n + d) * n + f] = val;
 }
 
+// Tiled slab materialisation: one block per (slab, u, v, d) evaluates the n^3
+// products for all (f, w, z) into shared memory, then writes each layout
+// with consecutive threads on consecutive addresses (n^2 doubles per row
+// segment for X1/X2, n for X3/X4).  The tile is [f][w][z] with odd strides
+// (n+1, n(n+1)+1 doubles), so every read pattern is free of bank conflicts.
+// With rmax, the block also folds the magnitudes into the row maxima of the
+// four layouts (bit patterns of non-negative doubles order like integers):
+// rmax[L * nslab n^3 + row] for layout L.
+constexpr int kSlabTileMax = 16 * (16 * 17 + 1);
+__global__ void __launch_bounds__(256) k_bamat_slabs_t(Rdm r, int s, const int *slab_cp, const int *slab_ap,
+                                                       int nslab, double *X1, double *X2, double *X3, double *X4,
+                                                       unsigned long long *rmax) {
+    __shared__ double tile[kSlabTileMax];
+    __shared__ double mwz[256];
+    const int n = r.n, sw = n + 1, sf = n * (n + 1) + 1;
+    const ll n2 = (ll)n * n, n3 = n2 * n, n6 = n3 * n3;
+    ll b = blockIdx.x;
+    const int d = (int)(b % n); b /= n;
+    const int v = (int)(b % n); b /= n;
+    const int u = (int)(b % n); b /= n;
+    const int sl = (int)b;
+    const int cp = slab_cp[sl], ap = slab_ap[sl];
+    for (int i = threadIdx.x; i < n3; i += blockDim.x) {
+        const int z = i % n, w = (i / n) % n, f = i / (int)n2;
+        tile[f * sf + w * sw + z] = r.eeee(cp + 1, ap + 1, u + 1, v + 1, d + 1, f + 1, w + 1, z + 1, s + 1);
+    }
+    __syncthreads();
+    const ll base = (ll)sl * n6;
+    for (int i = threadIdx.x; i < n3; i += blockDim.x) {
+        // X1 rows (u,v,z) cols (d,f,w): i = (z, f, w)
+        {
+            const int w = i % n, f = (i / n) % n, z = i / (int)n2;
+            X1[base + (((ll)u * n + v) * n + z) * n3 + ((ll)d * n + f) * n + w] = tile[f * sf + w * sw + z];
+        }
+        // X2 rows (u,v,w) cols (d,f,z): i = (w, f, z)
+        {
+            const int z = i % n, f = (i / n) % n, w = i / (int)n2;
+            X2[base + (((ll)u * n + v) * n + w) * n3 + ((ll)d * n + f) * n + z] = tile[f * sf + w * sw + z];
+        }
+        // X3 rows (u,w,z) cols (v,d,f), X4 rows (v,w,z) cols (u,d,f): i = (w, z, f)
+        {
+            const int f = i % n, z = (i / n) % n, w = i / (int)n2;
+            const double x = tile[f * sf + w * sw + z];
+            X3[base + (((ll)u * n + w) * n + z) * n3 + ((ll)v * n + d) * n + f] = x;
+            X4[base + (((ll)v * n + w) * n + z) * n3 + ((ll)u * n + d) * n + f] = x;
+        }
+    }
+    if (!rmax) return;
+    // m(w,z) = max_f |x|: the X3 / X4 partials; X1 (row z) = max_w, X2 (row w) = max_z
+    for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+        const int z = i % n, w = i / n;
+        double m = 0.0;
+        for (int f = 0; f < n; ++f) m = fmax(m, fabs(tile[f * sf + w * sw + z]));
+        mwz[i] = m;
+    }
+    __syncthreads();
+    const ll rows = (ll)nslab * n3, r0 = (ll)sl * n3;
+    for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+        const int z = i % n, w = i / n;
+        const unsigned long long m = (unsigned long long)__double_as_longlong(mwz[i]);
+        atomicMax(rmax + 2 * rows + r0 + ((ll)u * n + w) * n + z, m);
+        atomicMax(rmax + 3 * rows + r0 + ((ll)v * n + w) * n + z, m);
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double m1 = 0.0, m2 = 0.0;
+        for (int j = 0; j < n; ++j) {
+            m1 = fmax(m1, mwz[j * n + i]);  // row z = i: over w
+            m2 = fmax(m2, mwz[i * n + j]);  // row w = i: over z
+        }
+        atomicMax(rmax + 0 * rows + r0 + ((ll)u * n + v) * n + i, (unsigned long long)__double_as_longlong(m1));
+        atomicMax(rmax + 1 * rows + r0 + ((ll)u * n + v) * n + i, (unsigned long long)__double_as_longlong(m2));
+    }
+}
+
 // Integral operands (row-major [K, N]) from the Fortran atwo(n,n,n,n).
 __global__ void k_bamat_ints(const double *atwo, int n, double *A1, double *A2, double *A3) {
     ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
@@ -332,25 +406,29 @@ int launch_bamat_gemm(const Rdm &r, const double *atwo, const double *f, int nco
     int rc = 0;
     // split precision: digit workspace for a full batch of slabs
     void *ozw = nullptr;
+    unsigned long long *rmax = nullptr;  // row maxima of the four slab layouts (split digits)
     if (split) {
         oz::OzPlan pl(4, (ll)B * n3, (int)n3, n);
         if (cudaMallocAsync(&ozw, pl.bytes(), st) != cudaSuccess) return 2;
+        if (cudaMallocAsync((void **)&rmax, sizeof(unsigned long long) * 4 * (size_t)B * n3, st) != cudaSuccess)
+            return 2;
     }
     for (int s = 0; s < M && !rc; ++s) {
         for (int s0 = 0; s0 < n * n && !rc; s0 += B) {
             int nb = std::min(B, n * n - s0);
             double *X1 = X, *X2 = X + (ll)B * n6, *X3 = X2 + (ll)B * n6, *X4 = X3 + (ll)B * n6;
-            ll work = (ll)nb * n6;
-            k_bamat_slabs<<<(unsigned)((work + 255) / 256), 256, 0, st>>>(r, s, slabs + s0, slabs + n * n + s0, nb, X1,
-                                                                        X2, X3, X4);
-            g_launches.fetch_add(1, std::memory_order_relaxed);
             ll rows = (ll)nb * n3;
+            if (rmax) cudaMemsetAsync(rmax, 0, sizeof(unsigned long long) * 4 * (size_t)rows, st);
+            k_bamat_slabs_t<<<(unsigned)rows, 256, 0, st>>>(r, s, slabs + s0, slabs + n * n + s0, nb, X1, X2,
+                                                                   X3, X4, rmax);
+            g_launches.fetch_add(1, std::memory_order_relaxed);
             double *T1 = T + (ll)s0 * n4, *T2 = T + n6 + (ll)s0 * n4, *T3 = T + 2 * n6 + (ll)s0 * n4,
                    *T4 = T + 3 * n6 + (ll)s0 * n4;
             if (split) {
                 const double *Xs[4] = {X1, X2, X3, X4}, *As[4] = {A1, A2, A3, A3};
                 double *Ts[4] = {T1, T2, T3, T4};
-                rc |= oz::oz_gemm_skinny(oz::OzPlan(4, rows, (int)n3, n), Xs, As, Ts, n, n, ozw, st);
+                const unsigned long long *Rm[4] = {rmax, rmax + rows, rmax + 2 * rows, rmax + 3 * rows};
+                rc |= oz::oz_gemm_skinny(oz::OzPlan(4, rows, (int)n3, n), Xs, As, Ts, n, n, ozw, st, Rm);
                 continue;
             }
             rc |= dgemm_rm(handle.h, rows, n, n3, X1, A1, T1);
@@ -368,6 +446,7 @@ int launch_bamat_gemm(const Rdm &r, const double *atwo, const double *f, int nco
         // the product kernels share one error flag (a wait that timed out)
         if (!rc && oz::oz_check_error(ozw, st) != 0) rc = 5;
         cudaFreeAsync(ozw, st);
+        cudaFreeAsync(rmax, st);
     }
     cudaFreeAsync(slabs, st);
     cudaFreeAsync(X, st);

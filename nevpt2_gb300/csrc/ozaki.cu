@@ -320,7 +320,7 @@ __device__ __forceinline__ void digits(double x, int E, uint16_t (&d)[NSL]) {
 // 16-byte chunk (8 digits) of one row and octet per slice.  nrt * 128 rows
 // are written (zeros past `rows`).
 __global__ void __launch_bounds__(256) k_oz_split_rows(const double *X, long long rows, int K, int nkc, int nrt,
-                                                       uint8_t *ad, int *rexp) {
+                                                       uint8_t *ad, int *rexp, const unsigned long long *rmax) {
     __shared__ double smax[8][8];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, rr = lane & 7, ph = lane >> 3;
     const long long row = (long long)blockIdx.x * 8 + rr;
@@ -329,16 +329,20 @@ __global__ void __launch_bounds__(256) k_oz_split_rows(const double *X, long lon
     const double *xr = X + (valid ? row : 0) * (long long)K;
     const int noct = nkc * (KC / 8);
     double mx = 0.0;
-    if (valid)
-        for (int oct = ph + 4 * warp; oct * 8 < K; oct += 32)
-            for (int e = 0; e < 8 && oct * 8 + e < K; ++e) mx = fmax(mx, fabs(xr[oct * 8 + e]));
-    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, 8));
-    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
-    if (ph == 0) smax[warp][rr] = mx;
-    __syncthreads();
-    mx = 0.0;
+    if (rmax) {
+        mx = valid ? __longlong_as_double((long long)rmax[row]) : 0.0;
+    } else {
+        if (valid)
+            for (int oct = ph + 4 * warp; oct * 8 < K; oct += 32)
+                for (int e = 0; e < 8 && oct * 8 + e < K; ++e) mx = fmax(mx, fabs(xr[oct * 8 + e]));
+        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, 8));
+        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
+        if (ph == 0) smax[warp][rr] = mx;
+        __syncthreads();
+        mx = 0.0;
 #pragma unroll
-    for (int w = 0; w < 8; ++w) mx = fmax(mx, smax[w][rr]);
+        for (int w = 0; w < 8; ++w) mx = fmax(mx, smax[w][rr]);
+    }
     const int E = exp_above(mx);
     if (warp == 0 && ph == 0) rexp[row] = E;
     const int rt = (int)(row / BM), r = (int)(row % BM);
@@ -402,7 +406,7 @@ size_t OzPlan::bytes() const {
 }
 
 int oz_gemm_skinny(const OzPlan &pl, const double *const *X, const double *const *A, double *const *T, int lda,
-                   int ldt, void *work, cudaStream_t st) {
+                   int ldt, void *work, cudaStream_t st, const unsigned long long *const *rowmax) {
     if (pl.njob < 1 || pl.njob > 4 || pl.K < 1 || pl.K > kMaxK || pl.ncols < 1 || pl.ncols > NB) return 1;
     static bool attr_set = false;
     if (!attr_set) {
@@ -429,7 +433,7 @@ int oz_gemm_skinny(const OzPlan &pl, const double *const *X, const double *const
         int *cexp = (int *)w;
         w += 256;
         k_oz_split_rows<<<(unsigned)((long long)pl.nrt * BM / 8), 256, 0, st>>>(X[j], pl.rows, pl.K, pl.nkc, pl.nrt,
-                                                                              ad, rexp);
+                                                                              ad, rexp, rowmax ? rowmax[j] : nullptr);
         k_oz_split_cols<<<1, 256, 0, st>>>(A[j], pl.K, pl.ncols, lda, pl.nkc, bd, cexp);
         g_launches.fetch_add(2, std::memory_order_relaxed);
         b.job[j] = OzJob{ad, rexp, bd, cexp, T[j], pl.rows, pl.nrt};

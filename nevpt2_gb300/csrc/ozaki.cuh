@@ -68,8 +68,10 @@ struct OzPlan {
 // of device memory (16-byte aligned).  0 on success; nonzero for bad shapes
 // or launch failure.  The kernel's own error flag (a wait that timed out) is
 // read back by oz_check_error (synchronises `st`; 0 = fine, 4 = timeout).
+// rowmax (optional): per product, max_k |X[i,k]| of every row as the bit
+// pattern of the double (the split then skips its own pass over X).
 int oz_gemm_skinny(const OzPlan &pl, const double *const *X, const double *const *A, double *const *T, int lda,
-                   int ldt, void *work, cudaStream_t st);
+                   int ldt, void *work, cudaStream_t st, const unsigned long long *const *rowmax = nullptr);
 int oz_check_error(const void *work, cudaStream_t st);
 
 // General products (ozaki_wide.cu): C[m, n] (row-major, ldc) =
