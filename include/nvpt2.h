@@ -203,6 +203,15 @@ int nvpt_dgemm_split_ex_d(nvpt_context *ctx, int transa, int transb, int64_t m, 
                           const double *A, int64_t lda, const double *B, int64_t ldb, double beta, double *C,
                           int64_t ldc, void *stream);
 
+/* Householder tridiagonalisation on the device (no counterpart in the reference;
+ * the building block of the order-n^3 PC pencils of stage 2): A (n x n,
+ * column-major, symmetric, both triangles) -> d[n], e[n-1], tau[n-1] and the
+ * reflectors below the subdiagonal of A, in the output form of LAPACK
+ * dsytrd('L'): the diagonal and subdiagonal of A hold T (so that a
+ * dormtr('L') applies Q).  FP64 throughout.  NVPT_ETIMEDOUT if a grid
+ * barrier timed out. */
+int nvpt_sytrd_d(nvpt_context *ctx, int64_t n, double *A, double *d, double *e, double *tau, void *stream);
+
 /* No-allocation variant of nvpt_bamat_d -- no counterpart in the reference.
  * Same arguments and results (to rounding: its contractions sum in another
  * order), for callers that must not allocate device memory during a run:

@@ -79,6 +79,7 @@ _SIGS = {
     "nvpt_set_precision": ([P, ctypes.c_int], ctypes.c_int),
     "nvpt_get_precision": ([P], ctypes.c_int),
     "nvpt_dgemm_split_d": ([P, I64, I64, I64, P, P, P, P], ctypes.c_int),
+    "nvpt_sytrd_d": ([P, I64, P, P, P, P, P], ctypes.c_int),
     "nvpt_dgemm_split_ex_d": ([P, ctypes.c_int, ctypes.c_int, I64, I64, I64, ctypes.c_double, P, I64, P, I64,
                                ctypes.c_double, P, I64, P], ctypes.c_int),
     "nvpt_set_profiling": ([P, ctypes.c_int], ctypes.c_int),

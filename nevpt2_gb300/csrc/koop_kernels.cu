@@ -8,6 +8,8 @@
 // (bamat.cu); this file holds the n^5..n^7 work.
 #include "nvpt2_internal.h"
 
+#include <cublas_v2.h>
+
 namespace nvpt {
 
 #define ATWO(i, j, k, l) atwo[((i)-1) + (ll)n * (((j)-1) + (ll)n * (((k)-1) + (ll)n * ((l)-1)))]
@@ -209,6 +211,63 @@ __global__ void k_koop2E_ea(Rdm r, const double *atwo, const double *f, int ncor
         }
         O5(koopeaa, s, ap, bp, a, b) = acc;
     }
+}
+
+// The same 2-EA matrix as products.  Per state, the bracketed operands of
+// the reference's inner sum over (c, d, ie) are materialised as two n^3 x n^3
+// row blocks,
+//   G[(ap,bp,b), (c,d,ie)]       = -ro3t(ap,bp,ie,d,b,c) + 2[c=ie] ro2t(ap,bp,d,b)
+//                                  - 1/2 [d=ie] ro2t(ap,bp,c,b) - 1/2 [b=ie] ro2t(ap,bp,d,c)
+//   G[n^3 + (ap,bp,a), (c,d,ie)] = -ro3t(ap,bp,ie,a,d,c) + 2[c=ie] ro2t(ap,bp,a,d)
+//                                  - 1/2 [a=ie] ro2t(ap,bp,c,d) - 1/2 [d=ie] ro2t(ap,bp,a,c)
+// and one GEMM with A1[(c,d,ie), x] = atwo(c,ie,d,x) gives both contractions;
+// k_koop2E_ea_out adds the one-electron terms.  Indices 0-based, last fastest.
+__global__ void k_koop2E_ea_ops(Rdm r, int s, double *G) {
+    const int n = r.n;
+    const ll n3 = (ll)n * n * n, n6 = n3 * n3;
+    const ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 2 * n6) return;
+    const int half = (int)(t / n6);
+    const ll x = t % n6, col = x % n3, row = x / n3;
+    const int ie = (int)(col % n) + 1, d = (int)((col / n) % n) + 1, c = (int)(col / ((ll)n * n)) + 1;
+    const int z = (int)(row % n) + 1, bp = (int)((row / n) % n) + 1, ap = (int)(row / ((ll)n * n)) + 1;
+    double dum;
+    if (half == 0) {
+        const int b = z;
+        dum = -r.ro3t(ap, bp, ie, d, b, c, s);
+        if (c == ie) dum += 2.0 * r.ro2t(ap, bp, d, b, s);
+        if (d == ie) dum -= 0.5 * r.ro2t(ap, bp, c, b, s);
+        if (b == ie) dum -= 0.5 * r.ro2t(ap, bp, d, c, s);
+    } else {
+        const int a = z;
+        dum = -r.ro3t(ap, bp, ie, a, d, c, s);
+        if (c == ie) dum += 2.0 * r.ro2t(ap, bp, a, d, s);
+        if (a == ie) dum -= 0.5 * r.ro2t(ap, bp, c, d, s);
+        if (d == ie) dum -= 0.5 * r.ro2t(ap, bp, a, c, s);
+    }
+    G[t] = dum;
+}
+__global__ void k_koop2E_ea_ints(const double *atwo, int n, double *A1) {
+    const ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (ll)n * n * n * n) return;
+    const int x = (int)(t % n) + 1;
+    const ll k = t / n;
+    const int ie = (int)(k % n) + 1, d = (int)((k / n) % n) + 1, c = (int)(k / ((ll)n * n)) + 1;
+    A1[t] = ATWO(c, ie, d, x);
+}
+__global__ void k_koop2E_ea_out(Rdm r, int s, const double *f, int ncore, const double *P, double *koopeaa) {
+    const int n = r.n, M = r.M;
+    const ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+    const ll n4 = (ll)n * n * n * n;
+    if (t >= n4) return;
+    int x[4];
+    decode(t, n, 4, x);
+    const int ap = x[0], bp = x[1], a = x[2], b = x[3];
+    double acc = 0.0;
+    for (int c = 1; c <= n; ++c) acc += FF(a, c) * r.ro2t(ap, bp, c, b, s) + FF(b, c) * r.ro2t(ap, bp, a, c, s);
+    const ll pre = ((ll)(ap - 1) * n + (bp - 1)) * n;
+    acc += P[(pre + (b - 1)) * n + (a - 1)] + P[n4 + (pre + (a - 1)) * n + (b - 1)];
+    O5(koopeaa, s, ap, bp, a, b) = acc;
 }
 
 // src/koop_matrices.F90:433-541 koopman0pE, A (koopaa) and D (koopbb) of the
@@ -430,13 +489,49 @@ void launch_hrdm(const Rdm &r, double *hrdm, cudaStream_t st) {
     k_hrdm<<<blocks_for(n4, 256), 256, 0, st>>>(r, hrdm);
     g_launches.fetch_add(1, std::memory_order_relaxed);
 }
+namespace {
+struct KoopBlas {
+    cublasHandle_t h = nullptr;
+    ~KoopBlas() {
+        if (h) cublasDestroy(h);
+    }
+};
+}  // namespace
+
 void launch_koop2E(const Rdm &r, const double *atwo, const double *f, int ncore, double *ip2, double *ea2,
                    cudaStream_t st) {
-    ll n4 = (ll)r.n * r.n * r.n * r.n;
+    const int n = r.n;
+    const ll n3 = (ll)n * n * n, n4 = n3 * n, n6 = n3 * n3;
     k_koop2E_ip<<<blocks_for(n4, 64), 64, 0, st>>>(r, atwo, f, ncore, ip2);
     g_launches.fetch_add(1, std::memory_order_relaxed);
-    k_koop2E_ea<<<blocks_for(n4, 64), 64, 0, st>>>(r, atwo, f, ncore, ea2);
+    // 2-EA: operand blocks + one GEMM per state
+    static thread_local KoopBlas blas;
+    double *G = nullptr, *A1 = nullptr, *P = nullptr;
+    bool ok = (blas.h || cublasCreate(&blas.h) == CUBLAS_STATUS_SUCCESS) &&
+              cublasSetStream(blas.h, st) == CUBLAS_STATUS_SUCCESS &&
+              cudaMallocAsync((void **)&G, sizeof(double) * 2 * (size_t)n6, st) == cudaSuccess &&
+              cudaMallocAsync((void **)&A1, sizeof(double) * (size_t)n4, st) == cudaSuccess &&
+              cudaMallocAsync((void **)&P, sizeof(double) * 2 * (size_t)n4, st) == cudaSuccess;
+    if (!ok) {  // no room for the operand blocks: the per-element kernel
+        if (G) cudaFreeAsync(G, st);
+        if (A1) cudaFreeAsync(A1, st);
+        k_koop2E_ea<<<blocks_for(n4, 64), 64, 0, st>>>(r, atwo, f, ncore, ea2);
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+        return;
+    }
+    k_koop2E_ea_ints<<<blocks_for(n4, 256), 256, 0, st>>>(atwo, n, A1);
     g_launches.fetch_add(1, std::memory_order_relaxed);
+    const double one = 1.0, zero = 0.0;
+    for (int s = 1; s <= r.M; ++s) {
+        k_koop2E_ea_ops<<<blocks_for(2 * n6, 256), 256, 0, st>>>(r, s, G);
+        // row-major P[2 n^3, n] = G[2 n^3, n^3] A1[n^3, n]
+        cublasDgemm(blas.h, CUBLAS_OP_N, CUBLAS_OP_N, n, (int)(2 * n3), (int)n3, &one, A1, n, G, (int)n3, &zero, P, n);
+        k_koop2E_ea_out<<<blocks_for(n4, 256), 256, 0, st>>>(r, s, f, ncore, P, ea2);
+        g_launches.fetch_add(2, std::memory_order_relaxed);
+    }
+    cudaFreeAsync(G, st);
+    cudaFreeAsync(A1, st);
+    cudaFreeAsync(P, st);
 }
 void launch_koop0p(const Rdm &r, const double *atwo, const double *f, int ncore, double *gk0pa, double *gk0pd,
                    double *gk0pf, cudaStream_t st) {

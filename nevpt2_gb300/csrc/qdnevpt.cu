@@ -1803,7 +1803,7 @@ extern "C" int nvpt_qdnevpt(nvpt_context *ctx, const nvpt_qdnevpt_in *in, nvpt_q
         return rc;
     } catch (const Error &e) {
         nvpt_context_error_set(ctx, e.what());
-        return e.code == 3 ? NVPT_ENOMEM : (e.code == NVPT_EINVAL ? NVPT_EINVAL : NVPT_ECUDA);
+        return e.code == 3 ? NVPT_ENOMEM : e.code == 4 ? NVPT_ETIMEDOUT : (e.code == NVPT_EINVAL ? NVPT_EINVAL : NVPT_ECUDA);
     }
 }
 
@@ -1817,6 +1817,6 @@ extern "C" int nvpt_qdnevpt_d(nvpt_context *ctx, const nvpt_qdnevpt_in *in, nvpt
         return rc;
     } catch (const Error &e) {
         nvpt_context_error_set(ctx, e.what());
-        return e.code == 3 ? NVPT_ENOMEM : (e.code == NVPT_EINVAL ? NVPT_EINVAL : NVPT_ECUDA);
+        return e.code == 3 ? NVPT_ENOMEM : e.code == 4 ? NVPT_ETIMEDOUT : (e.code == NVPT_EINVAL ? NVPT_EINVAL : NVPT_ECUDA);
     }
 }

@@ -457,18 +457,14 @@ bool pencil_tridiag(Ctx &c, const double *K, const double *S, long long n, Penci
     P.tau = alloc(c, {n}, true);
     symmetrize_upper(c, S, n, P.U.p);
     symmetrize_upper(c, K, n, P.A.p);
-    int lw_p = 0, lw_t = 0;
+    int lw_p = 0;
     ck(cusolverDnDpotrf_bufferSize(c.sol, CUBLAS_FILL_MODE_UPPER, N, P.U.p, N, &lw_p), "potrf_bufferSize");
-    ck(cusolverDnDsytrd_bufferSize(c.sol, CUBLAS_FILL_MODE_UPPER, N, P.A.p, N, P.d.p, P.e.p, P.tau.p, &lw_t),
-       "sytrd_bufferSize");
-    SolverWork sw(c, lw_p > lw_t ? lw_p : lw_t);
+    SolverWork sw(c, lw_p);
     ck(cusolverDnDpotrf(c.sol, CUBLAS_FILL_MODE_UPPER, N, P.U.p, N, sw.w, lw_p, sw.info), "potrf");
     if (sw.status() != 0) return false;
     reduce_to_standard(c, P.A.p, P.U.p, n);
-    ck(cusolverDnDsytrd(c.sol, CUBLAS_FILL_MODE_UPPER, N, P.A.p, N, P.d.p, P.e.p, P.tau.p, sw.w, lw_t, sw.info),
-       "sytrd");
-    const int st = sw.status();
-    if (st != 0) throw Error(2, "sytrd failed, info=" + std::to_string(st));
+    if (sytrd_lower(c, P.A.p, n, P.d.p, P.e.p, P.tau.p, true) != 0)
+        throw Error(4, "tridiagonalisation: a grid barrier timed out");
     return true;
 }
 
@@ -480,11 +476,11 @@ void pencil_rhs(Ctx &c, const PencilTridiag &P, double *Y, long long m) {
                    P.U.p, N, Y, N),
        "trsm");
     int lw = 0;
-    ck(cusolverDnDormtr_bufferSize(c.sol, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, N, Mc, P.A.p, N,
+    ck(cusolverDnDormtr_bufferSize(c.sol, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, N, Mc, P.A.p, N,
                                    P.tau.p, Y, N, &lw),
        "ormtr_bufferSize");
     SolverWork sw(c, lw);
-    ck(cusolverDnDormtr(c.sol, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, N, Mc, P.A.p, N, P.tau.p, Y, N,
+    ck(cusolverDnDormtr(c.sol, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, N, Mc, P.A.p, N, P.tau.p, Y, N,
                         sw.w, lw, sw.info),
        "ormtr");
     const int st = sw.status();

@@ -134,6 +134,11 @@ struct PencilTridiag {
 bool pencil_tridiag(Ctx &c, const double *K, const double *S, long long n, PencilTridiag &P);
 // Upper triangle of A (column-major, symmetric) <- that of U^-T A U^-1.
 void reduce_to_standard(Ctx &c, double *A, const double *U, long long n);
+// Householder tridiagonalisation of the symmetric A (column-major; both
+// triangles valid, or only the upper one with upper_valid) in the output
+// form of dsytrd('L'): d[n], e[n-1], tau[n-1], reflectors below the
+// subdiagonal of A (tridiag.cu).  0, or 4 if a grid barrier timed out.
+int sytrd_lower(Ctx &c, double *A, long long n, double *d, double *e, double *tau, bool upper_valid);
 // Y <- Q^T U^-T Y for Y column-major [n, m] (= row-major [m, n]): each row
 // z of the row-major view becomes y with z^T (K + s S)^-1 z = y^T (T + s)^-1 y.
 void pencil_rhs(Ctx &c, const PencilTridiag &P, double *Y, long long m);
