@@ -333,6 +333,100 @@ __global__ void k_koop0p_ad(Rdm r, const double *atwo, const double *f, int ncor
     }
 }
 
+// The same A and D of the 0' class as products.  Per state, the operands of
+// the reference's sums over (c, d, ie) are materialised as four n^3 x n^3
+// blocks (rows (bp,ap,z), columns (c,d,ie), ie fastest):
+//   0: eee2(bp,ap,c,ie,d,z) + eee2(bp,ap,d,z,c,ie)             (A, z = b) x atwo(c,ie,d,a)
+//   1: the D operand of the atwo(c,ie,d,a) term               (D, z = b) x atwo(c,ie,d,a)
+//   2: eee2(bp,ap,z,ie,c,d) + eee2(bp,ap,c,d,z,ie)             (A, z = a) x atwo(b,ie,c,d)
+//   3: the D operand of the atwo(c,ie,b,d) term               (D, z = a) x atwo(c,ie,b,d)
+// and three GEMMs give the n^7 sums; k_koop0p_out adds the n^5 one-electron
+// terms, with the signs and halves of the reference.
+__device__ __forceinline__ double koop0p_e1(const Rdm &r, int c, int d, int ie, int bp, int ap, int a, int s) {
+    double e1 = -r.eee2(c, ie, a, ap, bp, d, s) - r.eee2(a, ap, bp, d, c, ie, s);
+    if (ap == a) e1 += 2.0 * (r.ee2(c, ie, bp, d, s) + r.ee2(bp, d, c, ie, s));
+    if (bp == ap) e1 += r.ee2(c, ie, a, d, s) + r.ee2(a, d, c, ie, s);
+    if (ap == c) {
+        e1 -= r.ee2(a, ie, bp, d, s);
+        if (ie == a) e1 += 2.0 * r.D1(s, bp, d);
+    }
+    if (bp == ie) {
+        e1 += r.ee2(a, ap, c, d, s);
+        if (ap == a) e1 -= 2.0 * r.D1(s, c, d);
+    }
+    return e1;
+}
+__device__ __forceinline__ double koop0p_e2(const Rdm &r, int c, int d, int ie, int bp, int ap, int b, int s) {
+    double e2 = -r.eee2(c, ie, d, ap, bp, b, s) - r.eee2(d, ap, bp, b, c, ie, s);
+    if (ap == d) e2 += 2.0 * (r.ee2(c, ie, bp, b, s) + r.ee2(bp, b, c, ie, s));
+    if (bp == ap) e2 += r.ee2(c, ie, d, b, s) + r.ee2(d, b, c, ie, s);
+    if (ap == c) {
+        e2 -= r.ee2(d, ie, bp, b, s);
+        if (d == ie) e2 += 2.0 * r.D1(s, bp, b);
+    }
+    if (bp == ie) {
+        e2 += r.ee2(d, ap, c, b, s);
+        if (d == ap) e2 -= 2.0 * r.D1(s, c, b);
+    }
+    return e2;
+}
+__global__ void k_koop0p_ops(Rdm r, int s, double *G) {
+    const int n = r.n;
+    const ll n3 = (ll)n * n * n, n6 = n3 * n3;
+    const ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 4 * n6) return;
+    const int blk = (int)(t / n6);
+    const ll x = t % n6, col = x % n3, row = x / n3;
+    const int ie = (int)(col % n) + 1, d = (int)((col / n) % n) + 1, c = (int)(col / ((ll)n * n)) + 1;
+    const int z = (int)(row % n) + 1, ap = (int)((row / n) % n) + 1, bp = (int)(row / ((ll)n * n)) + 1;
+    double v;
+    if (blk == 0) v = r.eee2(bp, ap, c, ie, d, z, s) + r.eee2(bp, ap, d, z, c, ie, s);
+    else if (blk == 1) v = koop0p_e2(r, c, d, ie, bp, ap, z, s);
+    else if (blk == 2) v = r.eee2(bp, ap, z, ie, c, d, s) + r.eee2(bp, ap, c, d, z, ie, s);
+    else v = koop0p_e1(r, c, d, ie, bp, ap, z, s);
+    G[t] = v;
+}
+// A2[(c,d,ie), x] = atwo(x,ie,c,d), A3[(c,d,ie), x] = atwo(c,ie,x,d)
+__global__ void k_koop0p_ints(const double *atwo, int n, double *A2, double *A3) {
+    const ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (ll)n * n * n * n) return;
+    const int x = (int)(t % n) + 1;
+    const ll k = t / n;
+    const int ie = (int)(k % n) + 1, d = (int)((k / n) % n) + 1, c = (int)(k / ((ll)n * n)) + 1;
+    A2[t] = ATWO(x, ie, c, d);
+    A3[t] = ATWO(c, ie, x, d);
+}
+__global__ void k_koop0p_out(Rdm r, int s, const double *f, int ncore, const double *P01, const double *P2,
+                             const double *P3, double *koopaa, double *koopbb) {
+    const int n = r.n, M = r.M;
+    const ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+    const ll n3 = (ll)n * n * n, n4 = n3 * n;
+    if (t >= n4) return;
+    int x[4];
+    decode(t, n, 4, x);
+    const int bp = x[0], ap = x[1], a = x[2], b = x[3];
+    double A = 0.0, Dm = 0.0;
+    for (int c = 1; c <= n; ++c) {
+        const double fca = FF(c, a), fbc = FF(b, c);
+        A += 2.0 * (fca * r.ee2(bp, ap, c, b, s) - fbc * r.ee2(bp, ap, a, c, s));
+    }
+    for (int c = 1; c <= n; ++c) {
+        const double fca = FF(c, a), fbc = FF(b, c);
+        double dum1 = -r.ee2(a, ap, bp, c, s);
+        if (a == ap) dum1 += 2.0 * r.D1(s, bp, c);
+        if (bp == ap) dum1 += r.D1(s, a, c);
+        double dum2 = -r.ee2(c, ap, bp, b, s);
+        if (ap == c) dum2 += 2.0 * r.D1(s, bp, b);
+        if (bp == ap) dum2 += r.D1(s, c, b);
+        Dm += -fbc * dum1 + fca * dum2;
+    }
+    const ll rb = ((ll)(bp - 1) * n + (ap - 1)) * n + (b - 1), ra = ((ll)(bp - 1) * n + (ap - 1)) * n + (a - 1);
+    A += P01[rb * n + (a - 1)] - P2[ra * n + (b - 1)];
+    Dm += -0.5 * P3[ra * n + (b - 1)] + 0.5 * P01[(n3 + rb) * n + (a - 1)];
+    O5(koopaa, s, bp, ap, a, b) = A;
+    O5(koopbb, s, bp, ap, a, b) = Dm;
+}
+
 // src/koop_matrices.F90:546-571 koopman0pE, F (koopab).  Thread per (a,b).
 __global__ void k_koop0p_f(Rdm r, const double *atwo, const double *f, int ncore, double *koopab) {
     const int n = r.n, M = r.M;
@@ -417,6 +511,78 @@ __global__ void k_bcmat(Rdm r, const double *atwo, const double *f, int ncore, d
         O5(cmat, s, ap, a, b, c) = C;
         O5(ctmat, s, ap, a, b, c) = Ct;
     }
+}
+
+// The same C / C~ matrices as products.  Per state, the operands of the n^7
+// sums over (d, ief, ie) are materialised as six n^3 x n^3 blocks (rows
+// (ap,u,w), columns (d,ief,ie), ie fastest), eee2 for C and eee2tl for C~:
+//   0/1: e(ap,u,d,ief,ie,w), u = b, w = c     x atwo(d,ief,ie,a)
+//   2/3: e(ap,u,d,ief,w,ie), u = b, w = a     x atwo(d,ief,c,ie)
+//   4/5: e(ap,ie,d,ief,u,w), u = a, w = c     x atwo(d,ief,b,ie)
+// three GEMMs (the C and C~ blocks stacked) give them; k_bcmat_out adds the
+// one-electron and n^6 terms in the reference's form.
+__global__ void k_bcmat_ops(Rdm r, int s, double *G) {
+    const int n = r.n;
+    const ll n3 = (ll)n * n * n, n6 = n3 * n3;
+    const ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 6 * n6) return;
+    const int blk = (int)(t / n6);
+    const ll x = t % n6, col = x % n3, row = x / n3;
+    const int ie = (int)(col % n) + 1, ief = (int)((col / n) % n) + 1, d = (int)(col / ((ll)n * n)) + 1;
+    const int w = (int)(row % n) + 1, u = (int)((row / n) % n) + 1, ap = (int)(row / ((ll)n * n)) + 1;
+    double v;
+    switch (blk) {
+    case 0: v = r.eee2(ap, u, d, ief, ie, w, s); break;
+    case 1: v = r.eee2tl(ap, u, d, ief, ie, w, s); break;
+    case 2: v = r.eee2(ap, u, d, ief, w, ie, s); break;
+    case 3: v = r.eee2tl(ap, u, d, ief, w, ie, s); break;
+    case 4: v = r.eee2(ap, ie, d, ief, u, w, s); break;
+    default: v = r.eee2tl(ap, ie, d, ief, u, w, s); break;
+    }
+    G[t] = v;
+}
+// B1[(d,ief,ie), x] = atwo(d,ief,ie,x), B2[(d,ief,ie), x] = atwo(d,ief,x,ie)
+__global__ void k_bcmat_ints(const double *atwo, int n, double *B1, double *B2) {
+    const ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (ll)n * n * n * n) return;
+    const int x = (int)(t % n) + 1;
+    const ll k = t / n;
+    const int ie = (int)(k % n) + 1, ief = (int)((k / n) % n) + 1, d = (int)(k / ((ll)n * n)) + 1;
+    B1[t] = ATWO(d, ief, ie, x);
+    B2[t] = ATWO(d, ief, x, ie);
+}
+__global__ void k_bcmat_out(Rdm r, int s, const double *atwo, const double *f, int ncore, const double *P,
+                            double *cmat, double *ctmat) {
+    const int n = r.n, M = r.M;
+    const ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+    const ll n3 = (ll)n * n * n, n4 = n3 * n;
+    if (t >= n4) return;
+    int x[4];
+    decode(t, n, 4, x);
+    const int ap = x[0], a = x[1], b = x[2], c = x[3];
+    double C = 0.0, Ct = 0.0;
+    for (int d = 1; d <= n; ++d) {
+        const double fda = FF(d, a), fcd = FF(c, d), fbd = FF(b, d);
+        C += fda * r.ee2(ap, b, d, c, s) - fcd * r.ee2(ap, b, a, d, s) - fbd * r.ee2(ap, d, a, c, s);
+        Ct += fda * r.ee2t(ap, b, d, c, s) - fcd * r.ee2t(ap, b, a, d, s) + fbd * r.ee2t(ap, d, a, c, s);
+        for (int ie = 1; ie <= n; ++ie) {
+            const double dint1 = ATWO(c, ie, d, a), dint2 = ATWO(d, ie, ie, a);
+            const double dint3 = ATWO(c, d, d, ie), dint4 = ATWO(b, d, d, ie);
+            C += r.ee2(ap, b, d, ie, s) * dint1 -
+                 0.5 * (r.ee2(ap, b, d, c, s) * dint2 + r.ee2(ap, b, a, ie, s) * dint3 - r.ee2(ap, ie, a, c, s) * dint4);
+            Ct += r.ee2t(ap, b, d, ie, s) * dint1 -
+                  0.5 * (r.ee2t(ap, b, d, c, s) * dint2 + r.ee2t(ap, b, a, ie, s) * dint3 -
+                         r.ee2t(ap, ie, a, c, s) * dint4);
+        }
+    }
+    // P: [3 GEMMs][2 n^3 rows (C block, C~ block)][n]
+    const ll rbc = ((ll)(ap - 1) * n + (b - 1)) * n + (c - 1), rba = ((ll)(ap - 1) * n + (b - 1)) * n + (a - 1);
+    const ll rac = ((ll)(ap - 1) * n + (a - 1)) * n + (c - 1);
+    const double *P1 = P, *P2 = P + 2 * n4, *P3 = P + 4 * n4;
+    C += P1[rbc * n + (a - 1)] - P2[rba * n + (c - 1)] - P3[rac * n + (b - 1)];
+    Ct += P1[(n3 + rbc) * n + (a - 1)] - P2[(n3 + rba) * n + (c - 1)] + P3[(n3 + rac) * n + (b - 1)];
+    O5(cmat, s, ap, a, b, c) = C;
+    O5(ctmat, s, ap, a, b, c) = Ct;
 }
 
 // src/koopro4QD.F90:4399-4459 bdmat.  Thread per (ap,a); EA part uses aj.
@@ -535,9 +701,42 @@ void launch_koop2E(const Rdm &r, const double *atwo, const double *f, int ncore,
 }
 void launch_koop0p(const Rdm &r, const double *atwo, const double *f, int ncore, double *gk0pa, double *gk0pd,
                    double *gk0pf, cudaStream_t st) {
-    ll n4 = (ll)r.n * r.n * r.n * r.n;
-    k_koop0p_ad<<<blocks_for(n4, 64), 64, 0, st>>>(r, atwo, f, ncore, gk0pa, gk0pd);
-    g_launches.fetch_add(1, std::memory_order_relaxed);
+    const int n = r.n;
+    const ll n3 = (ll)n * n * n, n4 = n3 * n, n6 = n3 * n3;
+    static thread_local KoopBlas blas;
+    double *G = nullptr, *Ai = nullptr, *P = nullptr;
+    const bool ok = (blas.h || cublasCreate(&blas.h) == CUBLAS_STATUS_SUCCESS) &&
+                    cublasSetStream(blas.h, st) == CUBLAS_STATUS_SUCCESS &&
+                    cudaMallocAsync((void **)&G, sizeof(double) * 4 * (size_t)n6, st) == cudaSuccess &&
+                    cudaMallocAsync((void **)&Ai, sizeof(double) * 3 * (size_t)n4, st) == cudaSuccess &&
+                    cudaMallocAsync((void **)&P, sizeof(double) * 4 * (size_t)n4, st) == cudaSuccess;
+    if (ok) {
+        double *A1 = Ai, *A2 = Ai + n4, *A3 = Ai + 2 * n4;
+        k_koop2E_ea_ints<<<blocks_for(n4, 256), 256, 0, st>>>(atwo, n, A1);
+        k_koop0p_ints<<<blocks_for(n4, 256), 256, 0, st>>>(atwo, n, A2, A3);
+        g_launches.fetch_add(2, std::memory_order_relaxed);
+        const double one = 1.0, zero = 0.0;
+        for (int s = 1; s <= r.M; ++s) {
+            k_koop0p_ops<<<blocks_for(4 * n6, 256), 256, 0, st>>>(r, s, G);
+            // row-major P01[2 n^3, n] = G[0:2 n^3] A1; P2 = G[2 n^3:3 n^3] A2; P3 = G[3 n^3:] A3
+            cublasDgemm(blas.h, CUBLAS_OP_N, CUBLAS_OP_N, n, (int)(2 * n3), (int)n3, &one, A1, n, G, (int)n3, &zero,
+                        P, n);
+            cublasDgemm(blas.h, CUBLAS_OP_N, CUBLAS_OP_N, n, (int)n3, (int)n3, &one, A2, n, G + 2 * n6, (int)n3, &zero,
+                        P + 2 * n4, n);
+            cublasDgemm(blas.h, CUBLAS_OP_N, CUBLAS_OP_N, n, (int)n3, (int)n3, &one, A3, n, G + 3 * n6, (int)n3, &zero,
+                        P + 3 * n4, n);
+            k_koop0p_out<<<blocks_for(n4, 256), 256, 0, st>>>(r, s, f, ncore, P, P + 2 * n4, P + 3 * n4, gk0pa, gk0pd);
+            g_launches.fetch_add(2, std::memory_order_relaxed);
+        }
+        cudaFreeAsync(G, st);
+        cudaFreeAsync(Ai, st);
+        cudaFreeAsync(P, st);
+    } else {  // no room for the operand blocks: the per-element kernel
+        if (G) cudaFreeAsync(G, st);
+        if (Ai) cudaFreeAsync(Ai, st);
+        k_koop0p_ad<<<blocks_for(n4, 64), 64, 0, st>>>(r, atwo, f, ncore, gk0pa, gk0pd);
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+    }
     k_koop0p_f<<<blocks_for((ll)r.n * r.n, 64), 64, 0, st>>>(r, atwo, f, ncore, gk0pf);
     g_launches.fetch_add(1, std::memory_order_relaxed);
 }
@@ -549,9 +748,38 @@ void launch_bbmat(const Rdm &r, const double *atwo, const double *f, const doubl
 }
 void launch_bcmat(const Rdm &r, const double *atwo, const double *f, int ncore, double *c, double *ct,
                   cudaStream_t st) {
-    ll n4 = (ll)r.n * r.n * r.n * r.n;
-    k_bcmat<<<blocks_for(n4, 64), 64, 0, st>>>(r, atwo, f, ncore, c, ct);
+    const int n = r.n;
+    const ll n3 = (ll)n * n * n, n4 = n3 * n, n6 = n3 * n3;
+    static thread_local KoopBlas blas;
+    double *G = nullptr, *Bi = nullptr, *P = nullptr;
+    const bool ok = (blas.h || cublasCreate(&blas.h) == CUBLAS_STATUS_SUCCESS) &&
+                    cublasSetStream(blas.h, st) == CUBLAS_STATUS_SUCCESS &&
+                    cudaMallocAsync((void **)&G, sizeof(double) * 6 * (size_t)n6, st) == cudaSuccess &&
+                    cudaMallocAsync((void **)&Bi, sizeof(double) * 2 * (size_t)n4, st) == cudaSuccess &&
+                    cudaMallocAsync((void **)&P, sizeof(double) * 6 * (size_t)n4, st) == cudaSuccess;
+    if (!ok) {  // no room for the operand blocks: the per-element kernel
+        if (G) cudaFreeAsync(G, st);
+        if (Bi) cudaFreeAsync(Bi, st);
+        k_bcmat<<<blocks_for(n4, 64), 64, 0, st>>>(r, atwo, f, ncore, c, ct);
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+        return;
+    }
+    double *B1 = Bi, *B2 = Bi + n4;
+    k_bcmat_ints<<<blocks_for(n4, 256), 256, 0, st>>>(atwo, n, B1, B2);
     g_launches.fetch_add(1, std::memory_order_relaxed);
+    const double one = 1.0, zero = 0.0;
+    const double *Bs[3] = {B1, B2, B2};
+    for (int s = 1; s <= r.M; ++s) {
+        k_bcmat_ops<<<blocks_for(6 * n6, 256), 256, 0, st>>>(r, s, G);
+        for (int g = 0; g < 3; ++g)  // row-major P_g[2 n^3, n] = G[blocks 2g, 2g+1] B_g
+            cublasDgemm(blas.h, CUBLAS_OP_N, CUBLAS_OP_N, n, (int)(2 * n3), (int)n3, &one, Bs[g], n, G + 2 * g * n6,
+                        (int)n3, &zero, P + 2 * g * n4, n);
+        k_bcmat_out<<<blocks_for(n4, 256), 256, 0, st>>>(r, s, atwo, f, ncore, P, c, ct);
+        g_launches.fetch_add(2, std::memory_order_relaxed);
+    }
+    cudaFreeAsync(G, st);
+    cudaFreeAsync(Bi, st);
+    cudaFreeAsync(P, st);
 }
 void launch_bdmat(const Rdm &r, const double *atwo, const double *f, const double *aj, int ncore, double *d,
                   double *dt, cudaStream_t st) {
