@@ -55,6 +55,10 @@ def _args():
                     help="run only --warmup + --steps device-resident steps, untimed (for ncu launch lists)")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "split"],
                     help="contraction precision of the --profile steps")
+    ap.add_argument("--sytrd", type=int, metavar="N",
+                    help="time the device tridiagonalisation of a symmetric matrix of order N and exit")
+    ap.add_argument("--oz-wide", nargs=3, type=int, metavar=("M", "N", "K"),
+                    help="time the general split-precision product C = A^T B (M x N, inner K) and exit")
     ap.add_argument("--oz-gemm", nargs=3, type=int, metavar=("ROWS", "K", "N"),
                     help="time the split-precision product kernel alone on a random ROWS x K by K x N problem")
     return ap.parse_args()
@@ -89,6 +93,70 @@ def run_oz_gemm(args):
     per = ms.value / max(cnt.value, 1)
     print(json.dumps({"oz_gemm": [m, k, n], "launches": cnt.value, "ms_per_launch": per,
                       "gbs": by.value / cnt.value / (per * 1e-3) / 1e9, "rel_err": err}), flush=True)
+
+
+def run_oz_wide(args):
+    """The general split-precision product (nvpt_dgemm_split_ex_d, C = A^T A
+    shaped like the stage's (i r|j s) blocks when M = N) on random operands:
+    one warm-up call, then --steps calls; prints the product kernel's device
+    time (CUDA events inside the library) and its BF16 digit-product rate."""
+    import ctypes
+
+    import torch
+
+    from nevpt2_gb300 import koopro
+    from nevpt2_gb300._native import ptr
+    m, n, k = args.oz_wide
+    dev = torch.device("cuda", 0)
+    g = torch.Generator(device=dev)
+    g.manual_seed(8)
+    A = torch.randn(k, m, dtype=torch.float64, device=dev, generator=g)
+    B = torch.randn(k, n, dtype=torch.float64, device=dev, generator=g)
+    C = torch.empty(m, n, dtype=torch.float64, device=dev)
+    ctx = koopro.context()
+    call = lambda: ctx.call("nvpt_dgemm_split_ex_d", 1, 0, m, n, k, 1.0, ptr(A), m, ptr(B), n, 0.0, ptr(C), n, None)
+    call()
+    ctx.call("nvpt_set_profiling", 1)
+    for _ in range(max(1, args.steps)):
+        call()
+    ms, cnt, fl = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
+    ctx.call("nvpt_profile_read", b"oz_wide", ctypes.byref(ms), ctypes.byref(cnt), ctypes.byref(fl))
+    ctx.call("nvpt_set_profiling", 0)
+    ref = A.t() @ B
+    err = float((C - ref).abs().max() / ref.abs().max())
+    per = ms.value / max(cnt.value, 1)
+    tf = fl.value / cnt.value / (per * 1e-3) / 1e12
+    print(json.dumps({"oz_wide": [m, n, k], "launches": cnt.value, "ms_per_launch": per,
+                      "fp64_equivalent_tflops": tf, "bf16_tflops": 64 * tf, "rel_err": err}), flush=True)
+
+
+def run_sytrd(args):
+    """The device tridiagonalisation (nvpt_sytrd_d) of a random symmetric
+    matrix of order N: one warm-up call, then --steps calls, CUDA events."""
+    import torch
+
+    from nevpt2_gb300 import koopro
+    from nevpt2_gb300._native import ptr
+    n = args.sytrd
+    dev = torch.device("cuda", 0)
+    g = torch.Generator(device=dev)
+    g.manual_seed(3)
+    X = torch.randn(n, n, dtype=torch.float64, device=dev, generator=g)
+    A0 = (X + X.t()) / 2
+    d, e, tau = (torch.zeros(n, dtype=torch.float64, device=dev) for _ in range(3))
+    ctx = koopro.context()
+    st = torch.cuda.current_stream(dev)
+    times = []
+    for it in range(1 + max(1, args.steps)):
+        A = A0.clone()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        ctx.call("nvpt_sytrd_d", n, ptr(A), ptr(d), ptr(e), ptr(tau), st.cuda_stream)
+        b.record(st)
+        torch.cuda.synchronize(dev)
+        if it:
+            times.append(a.elapsed_time(b))
+    print(json.dumps({"sytrd": n, "ms": float(np.median(times)), "ms_all": times}), flush=True)
 
 
 def _dist():
@@ -591,7 +659,11 @@ def live_ro4_entries(n: int) -> int:
 
 if __name__ == "__main__":
     a = _args()
-    if a.oz_gemm:
+    if a.sytrd:
+        run_sytrd(a)
+    elif a.oz_wide:
+        run_oz_wide(a)
+    elif a.oz_gemm:
         run_oz_gemm(a)
     elif a.impl == "reference":
         run_reference(a)

@@ -516,11 +516,19 @@ int nvpt_dgemm_split_ex_d(nvpt_context *ctx, int transa, int transb, int64_t m, 
                     "dgemm_split_ex: need m, n >= 1, 1 <= k <= 2^19, lda/ldb/ldc >= the row lengths, alpha = +-2^e");
     cudaStream_t st = pick(ctx, stream);
     oz::WideGemm g;
-    g.m = m; g.n = n; g.K = (int)k;
-    g.A = A; g.a_r = transa ? 1 : lda; g.a_k = transa ? lda : 1;
-    g.B = B; g.b_c = transb ? ldb : 1; g.b_k = transb ? 1 : ldb;
+    g.K = (int)k;
     g.alpha = alpha; g.beta = beta; g.C = C; g.ldc = ldc;
-    const size_t bytes = oz::oz_wide_bytes(m, n, (int)k) + 256;
+    if (m >= 64 || n < 128) {
+        g.m = m; g.n = n;
+        g.A = A; g.a_r = transa ? 1 : lda; g.a_k = transa ? lda : 1;
+        g.B = B; g.b_c = transb ? ldb : 1; g.b_k = transb ? 1 : ldb;
+    } else {  // few rows, many columns: C^T = op(B)^T op(A)^T fills the 128-row tiles
+        g.m = n; g.n = m;
+        g.A = B; g.a_r = transb ? ldb : 1; g.a_k = transb ? 1 : ldb;
+        g.B = A; g.b_c = transa ? 1 : lda; g.b_k = transa ? lda : 1;
+        g.c_trans = true;
+    }
+    const size_t bytes = oz::oz_wide_bytes(g.m, g.n, (int)k) + 256;
     void *w = nullptr;
     NV_TRY(cuda_check(ctx, cudaMallocAsync(&w, bytes, st), "dgemm_split_ex workspace"));
     int *err = (int *)((uint8_t *)w + bytes - 256);

@@ -91,6 +91,7 @@ struct WideGemm {
     double *C = nullptr;
     long long ldc = 0;
     bool lower = false;
+    bool c_trans = false;  // store C^T: element (i, j) at C[j * ldc + i]
 };
 constexpr int kWideMaxK = 1 << 19;  // keeps the 64-bit drain sums in range
 size_t oz_wide_bytes(long long m, long long n, int K);  // device workspace (16-byte aligned)

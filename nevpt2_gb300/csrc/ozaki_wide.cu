@@ -102,7 +102,7 @@ struct WideArgs {
     const int *rexp, *cexp;
     double *C;
     long long ldc, m, n;
-    int nrt, nct, nkc, lower;
+    int nrt, nct, nkc, lower, ctrans;
     double beta;
 };
 
@@ -301,15 +301,15 @@ __global__ void __launch_bounds__(W_THREADS, 1) k_oz_wide(WideArgs a, int *err) 
             const long long row = (long long)rt * BM + quad * 32 + lane;
             if (row < a.m) {
                 const int ei = a.rexp[row];
-                double *o = a.C + row * a.ldc;
 #pragma unroll
                 for (int c = 0; c < 16; ++c) {
                     const long long col = (long long)ct * NT + half * 16 + c;
                     if (col < a.n) {
                         const int e = ei + a.cexp[col];
                         double v = scale2((double)hi[c], e - 36) + scale2((double)lo[c], e - 72);
-                        if (a.beta != 0.0) v = fma(a.beta, o[col], v);
-                        o[col] = v;
+                        double *o = a.ctrans ? a.C + col * a.ldc + row : a.C + row * a.ldc + col;
+                        if (a.beta != 0.0) v = fma(a.beta, *o, v);
+                        *o = v;
                     }
                 }
             }
@@ -466,7 +466,8 @@ int oz_gemm_wide(const WideGemm &g, void *work, int *err, cudaStream_t st) {
     k_wide_split<<<dim3((unsigned)((long long)L.nct * NT / 32), (unsigned)L.nkc), 256, 0, st>>>(
         g.B, g.b_c, g.b_k, g.n, g.K, g.alpha, NT, L.nkc, cexp, bd);
     g_launches.fetch_add(4, std::memory_order_relaxed);
-    WideArgs a{ad, bd, rexp, cexp, g.C, g.ldc, g.m, g.n, L.nrt, L.nct, L.nkc, g.lower ? 1 : 0, g.beta};
+    WideArgs a{ad, bd, rexp, cexp, g.C, g.ldc, g.m, g.n, L.nrt, L.nct, L.nkc, g.lower ? 1 : 0, g.c_trans ? 1 : 0,
+               g.beta};
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

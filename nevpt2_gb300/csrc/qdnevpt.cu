@@ -152,61 +152,70 @@ __global__ void k_pc_finish(const double *R, const double *Rp, const double *Rj,
 }
 
 // PC sums of one class from the tridiagonal form of its pencil: for label l
-// (one thread each) with shift sig[l], x = (T + sig I)^-1 y_l by Gaussian
+// (one CTA each) with shift sig[l], x = (T + sig I)^-1 y_l by Gaussian
 // elimination with partial pivoting on the tridiagonal T (d[n], e[n-1]),
 // then
 //   acc[0] -= y_l . x,   acc[1] += x . x,   acc[2 + k] -= y_{k+1,l} . x,
 // which are the type-0 sums of k_pc_finish over the eigenpairs of T
 // (sum_mu r_mu^2 / (w_mu + sig) = y^T (T + sig)^-1 y with r = G^T y).
 // Y is row-major [n][ncol], column k L + l holding block k (0: own state,
-// k > 0: the other states) of label l.  Work arrays are [n][L] (label
-// fastest, so that the threads' accesses coalesce).
+// k > 0: the other states) of label l.  The CTA stages d, e and y_l in
+// shared memory; one thread runs the elimination and the back substitution
+// there (every step a shared-memory access, no global latency), then all
+// threads form the dot products.  Shared memory: 6 n doubles.
 __global__ void k_tridiag_resolvent(const double *d, const double *e, long long n, const double *Y, long long ncol,
-                                    long long L, int nother, const double *sig, double *wb, double *wc, double *wd,
-                                    double *wy, double *acc) {
-    const long long l = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    double en = 0.0, ps = 0.0;
-    double offs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    if (l < L && n > 0) {
+                                    long long L, int nother, const double *sig, double *acc) {
+    extern __shared__ double sm[];
+    double *sd = sm, *se = sm + n, *wb = sm + 2 * n, *wc = sm + 3 * n, *wd = sm + 4 * n, *wy = sm + 5 * n;
+    const long long l = blockIdx.x;
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+        sd[i] = d[i];
+        se[i] = i + 1 < n ? e[i] : 0.0;
+        wy[i] = Y[i * ncol + l];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
         const double s = sig[l];
-        auto at = [&](long long i) { return i * L + l; };
-        // row i: diagonal b, super-diagonal c, second super-diagonal (fill) dd
-        double b = d[0] + s, cc = n > 1 ? e[0] : 0.0, y = Y[l];
+        // row i: diagonal b, super-diagonal c; the fill of a row exchange goes to wd
+        double b = sd[0] + s, cc = se[0], y = wy[0];
         for (long long i = 0; i + 1 < n; ++i) {
-            const double a1 = e[i];                          // row i+1, column i
-            const double b1 = d[i + 1] + s;                  // row i+1, column i+1
-            const double c1 = i + 2 < n ? e[i + 1] : 0.0;    // row i+1, column i+2
-            const double y1 = Y[(i + 1) * ncol + l];
+            const double a1 = se[i];                        // row i+1, column i
+            const double b1 = sd[i + 1] + s;                // row i+1, column i+1
+            const double c1 = i + 2 < n ? se[i + 1] : 0.0;  // row i+1, column i+2
+            const double y1 = wy[i + 1];
             if (fabs(b) >= fabs(a1)) {  // keep row i as pivot row
                 const double f = a1 / b;
-                wb[at(i)] = b; wc[at(i)] = cc; wd[at(i)] = 0.0; wy[at(i)] = y;
+                wb[i] = b; wc[i] = cc; wd[i] = 0.0; wy[i] = y;
                 b = b1 - f * cc;
                 cc = c1;
                 y = y1 - f * y;
             } else {                    // interchange rows i and i+1
                 const double f = b / a1;
-                wb[at(i)] = a1; wc[at(i)] = b1; wd[at(i)] = c1; wy[at(i)] = y1;
+                wb[i] = a1; wc[i] = b1; wd[i] = c1; wy[i] = y1;
                 b = cc - f * b1;
                 cc = -f * c1;
                 y = y - f * y1;
             }
         }
-        wb[at(n - 1)] = b; wy[at(n - 1)] = y;
+        wb[n - 1] = b;
         // back substitution, x over wy
         double x2 = 0.0, x1 = y / b;
-        wy[at(n - 1)] = x1;
+        wy[n - 1] = x1;
         for (long long i = n - 2; i >= 0; --i) {
-            const double x = (wy[at(i)] - wc[at(i)] * x1 - wd[at(i)] * x2) / wb[at(i)];
-            wy[at(i)] = x;
+            const double x = (wy[i] - wc[i] * x1 - wd[i] * x2) / wb[i];
+            wy[i] = x;
             x2 = x1;
             x1 = x;
         }
-        for (long long i = 0; i < n; ++i) {
-            const double x = wy[at(i)];
-            en -= Y[i * ncol + l] * x;
-            ps += x * x;
-            for (int k = 0; k < nother && k < 8; ++k) offs[k] -= Y[i * ncol + (k + 1) * L + l] * x;
-        }
+    }
+    __syncthreads();
+    double en = 0.0, ps = 0.0;
+    double offs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+        const double x = wy[i];
+        en -= Y[i * ncol + l] * x;
+        ps += x * x;
+        for (int k = 0; k < nother && k < 8; ++k) offs[k] -= Y[i * ncol + (k + 1) * L + l] * x;
     }
     block_add(en, acc + 0);
     block_add(ps, acc + 1);
@@ -683,10 +692,12 @@ class Runner {
         T sg = upload(c, shift);
         T a = alloc(c, {2 + 8}, true);
         if (L > 0 && n > 0) {
-            T wb = alloc(c, {n, L}, false), wc = alloc(c, {n, L}, false), wd = alloc(c, {n, L}, false),
-              wy = alloc(c, {n, L}, false);
-            k_tridiag_resolvent<<<(unsigned)((L + 63) / 64), 64, 0, c.st>>>(PT.d.p, PT.e.p, n, Yt.p, Yt.sh[1], L, M - 1,
-                                                                            sg.p, wb.p, wc.p, wd.p, wy.p, a.p);
+            const size_t smem = sizeof(double) * 6 * (size_t)n;
+            if (smem > 227 * 1024) throw Error(NVPT_EINVAL, "resolvent: pencil order above the shared-memory limit");
+            ck(cudaFuncSetAttribute(k_tridiag_resolvent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+               "smem attr");
+            k_tridiag_resolvent<<<(unsigned)L, 128, smem, c.st>>>(PT.d.p, PT.e.p, n, Yt.p, Yt.sh[1], L, M - 1, sg.p,
+                                                                   a.p);
             LAUNCHED();
         }
         return download(c, a.p, 2 + 8);

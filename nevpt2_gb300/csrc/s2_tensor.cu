@@ -210,9 +210,11 @@ T permuted(Ctx &c, const T &in, const std::vector<int> &axes, double alpha) {
 }
 
 namespace {
-// Products big enough to pay for the digit splits; alpha = +-2^e.
+// Products big enough to pay for the digit splits; alpha = +-2^e.  A product
+// with few rows runs transposed (its columns fill the 128-row tiles).
 bool split_product(const Ctx &c, long long m, long long n, long long k, double alpha) {
-    if (!c.split || k < 64 || k > oz::kWideMaxK || m < 64 || n < 16) return false;
+    if (!c.split || k < 64 || k > oz::kWideMaxK) return false;
+    if (!((m >= 64 && n >= 16) || (m >= 16 && n >= 128))) return false;
     if ((double)m * (double)n * (double)k < 6.7e7) return false;
     int e = 0;
     return std::frexp(std::fabs(alpha), &e) == 0.5;
@@ -231,10 +233,18 @@ void gemm(Ctx &c, bool ta, bool tb, long long m, long long n, long long k, doubl
     if (m == 0 || n == 0) return;
     if (split_product(c, m, n, k, alpha)) {
         oz::WideGemm g;
-        g.m = m; g.n = n; g.K = (int)k;
-        g.A = A; g.a_r = ta ? 1 : lda; g.a_k = ta ? lda : 1;
-        g.B = B; g.b_c = tb ? ldb : 1; g.b_k = tb ? 1 : ldb;
+        g.K = (int)k;
         g.alpha = alpha; g.beta = beta; g.C = C; g.ldc = ldc;
+        if (m >= 64) {
+            g.m = m; g.n = n;
+            g.A = A; g.a_r = ta ? 1 : lda; g.a_k = ta ? lda : 1;
+            g.B = B; g.b_c = tb ? ldb : 1; g.b_k = tb ? 1 : ldb;
+        } else {  // C^T = op(B)^T op(A)^T: rows of the product are the columns of C
+            g.m = n; g.n = m;
+            g.A = B; g.a_r = tb ? ldb : 1; g.a_k = tb ? 1 : ldb;
+            g.B = A; g.b_c = ta ? 1 : lda; g.b_k = ta ? lda : 1;
+            g.c_trans = true;
+        }
         split_gemm(c, g);
         return;
     }

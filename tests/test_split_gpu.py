@@ -136,7 +136,8 @@ def _bound_ex(X, Y):
 @pytest.mark.parametrize("m,n,k,ta,tb", [(128, 32, 64, False, False), (300, 77, 1184, False, False),
                                          (257, 500, 100, True, False), (1000, 1000, 4096, False, True),
                                          (33, 5, 3000, True, True), (7, 1, 1, False, False),
-                                         (640, 96, 1537, False, False)])
+                                         (640, 96, 1537, False, False), (30, 700, 1184, False, False),
+                                         (40, 512, 512, True, True)])
 def test_split_ex_within_bound(m, n, k, ta, tb):
     rng = np.random.default_rng(m + 3 * n + 7 * k)
     A = rng.standard_normal((k, m) if ta else (m, k))
