@@ -1585,6 +1585,7 @@ struct ClassStreams {
         for (auto &x : c) {
             x.split = false;
             x.oz_err = nullptr;
+            x.sm_share = 1;
         }
         CtxPool::release(c, dev);
     }
@@ -1716,10 +1717,14 @@ int run_qdnevpt(nvpt_context *ctx, cudaStream_t st, const nvpt_qdnevpt_in *in, n
     int dev = 0;
     ck(cudaGetDevice(&dev), "cudaGetDevice");
     ClassStreams ps((size_t)M), cs((size_t)M * nj);
+    // order-n^3 pencils in flight at once: one per state and (+-1') class
+    const int pencils = M * (((m & 64u) ? 1 : 0) + ((m & 32u) ? 1 : 0));
     for (auto *pool : {&ps, &cs})
         for (auto &pc_ : pool->c) {
             pc_.split = c.split;
             pc_.oz_err = c.oz_err;
+            // measured: 8 pencils (4 states) fastest on quarters; 2 pencils on the whole GPU each
+            pc_.sm_share = pc && pencils >= 4 ? 4 : 1;
         }
     ck(cudaEventRecord(ps.prep, c.st), "event");  // B and h ready
     std::vector<std::unique_ptr<Runner>> SR(M);

@@ -473,7 +473,7 @@ bool pencil_tridiag(Ctx &c, const double *K, const double *S, long long n, Penci
     ck(cusolverDnDpotrf(c.sol, CUBLAS_FILL_MODE_UPPER, N, P.U.p, N, sw.w, lw_p, sw.info), "potrf");
     if (sw.status() != 0) return false;
     reduce_to_standard(c, P.A.p, P.U.p, n);
-    if (sytrd_lower(c, P.A.p, n, P.d.p, P.e.p, P.tau.p, true) != 0)
+    if (sytrd_lower(c, P.A.p, n, P.d.p, P.e.p, P.tau.p, true, std::min(4, std::max(1, c.sm_share))) != 0)
         throw Error(4, "tridiagonalisation: a grid barrier timed out");
     return true;
 }

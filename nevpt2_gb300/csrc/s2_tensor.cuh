@@ -80,6 +80,9 @@ struct Ctx {
     // products on the tensor cores; a pipeline timeout sets *oz_err.
     bool split = false;
     int *oz_err = nullptr;
+    // Order-n^3 pencils tridiagonalised at the same time on other streams:
+    // each takes 1/sm_share of the SMs (at most 4), so that they overlap.
+    int sm_share = 1;
 };
 
 T alloc(Ctx &c, std::initializer_list<long long> shape, bool zero = true);
@@ -137,8 +140,10 @@ void reduce_to_standard(Ctx &c, double *A, const double *U, long long n);
 // Householder tridiagonalisation of the symmetric A (column-major; both
 // triangles valid, or only the upper one with upper_valid) in the output
 // form of dsytrd('L'): d[n], e[n-1], tau[n-1], reflectors below the
-// subdiagonal of A (tridiag.cu).  0, or 4 if a grid barrier timed out.
-int sytrd_lower(Ctx &c, double *A, long long n, double *d, double *e, double *tau, bool upper_valid);
+// subdiagonal of A (tridiag.cu); the panel kernels use 1/share of the SMs.
+// 0, or 4 if a grid barrier timed out.
+int sytrd_lower(Ctx &c, double *A, long long n, double *d, double *e, double *tau, bool upper_valid,
+                int share = 1);
 // Y <- Q^T U^-T Y for Y column-major [n, m] (= row-major [m, n]): each row
 // z of the row-major view becomes y with z^T (K + s S)^-1 z = y^T (T + s)^-1 y.
 void pencil_rhs(Ctx &c, const PencilTridiag &P, double *Y, long long m);

@@ -38,15 +38,14 @@ namespace {
 constexpr int NBP = 32;        // panel width
 constexpr int TT = 256;        // threads per CTA
 constexpr int PARTS = 2 + 2 * NBP;  // column sums: |x|^2, w.v, (W^T a, V^T a)[NBP]
-constexpr int kSmShare = 4;    // concurrent tridiagonalisations the GPU is split between (default)
-// NVPT_SYTRD_SHARE (1..16) overrides the split, for tuning on other parts.
-int sm_share() {
+// NVPT_SYTRD_SHARE (1..16) overrides the caller's SM split, for tuning on other parts.
+int sm_share(int share) {
     static const int v = [] {
         const char *e = std::getenv("NVPT_SYTRD_SHARE");
         const int x = e ? std::atoi(e) : 0;
-        return (x >= 1 && x <= 16) ? x : kSmShare;
+        return (x >= 1 && x <= 16) ? x : 0;
     }();
-    return v;
+    return v ? v : share;
 }
 constexpr unsigned kBarSpin = 1u << 22;  // polls (with back-off) before a barrier gives up
 
@@ -295,7 +294,7 @@ __global__ void k_mirror_to_lower(double *A, long long n) {
 
 }  // namespace
 
-int sytrd_lower(Ctx &c, double *A, long long n, double *d, double *e, double *tau, bool upper_valid) {
+int sytrd_lower(Ctx &c, double *A, long long n, double *d, double *e, double *tau, bool upper_valid, int share) {
     if (n <= 0) return 0;
     constexpr int TPB = 256;
     auto nb = [](long long x) { return (unsigned)((x + TPB - 1) / TPB); };
@@ -311,11 +310,11 @@ int sytrd_lower(Ctx &c, double *A, long long n, double *d, double *e, double *ta
     ck(cudaFuncSetAttribute(k_sytrd_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vbytes), "smem attr");
     ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sytrd_panel, TT, vbytes), "occupancy");
     if (per < 1) throw Error(2, "sytrd panel kernel cannot be resident");
-    // A quarter of the SMs per tridiagonalisation: the eight pencils of a QD
-    // step reach this point together on their own streams, and four of them
-    // then share the GPU -- the per-column barrier latency of one overlaps the
-    // FP64 products of the others.
-    const unsigned G = (unsigned)std::max(1, sms / sm_share());
+    // 1/share of the SMs per tridiagonalisation: the pencils of a QD step
+    // reach this point together on their own streams and then share the GPU
+    // -- the per-column barrier latency of one overlaps the FP64 products of
+    // the others.
+    const unsigned G = (unsigned)std::max(1, sms / std::max(1, sm_share(share)));
     T V = alloc(c, {NBP, n}, false), W = alloc(c, {NBP, n}, false), y = alloc(c, {n}, false);
     T accs = alloc(c, {2, PARTS}, true);  // zero: the first column of every panel has parity 0
     T barw = alloc(c, {2}, true);  // Bar (12 bytes) in 16 zeroed bytes
