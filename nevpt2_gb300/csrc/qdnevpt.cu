@@ -9,8 +9,11 @@
 // threshold rules; every partially contracted (PC) class runs the metric
 // pseudo-inverse sequence (syevd, drop eigenvalues < thr, X = U w^-1/2,
 // K~ = X^T K X, syevd, C = X V; caux0p :4744) and then its energy sums as
-// GEMMs over (label, mu) with a finishing kernel.  Energies accumulate in FP64
-// on the device.
+// GEMMs over (label, mu) with a finishing kernel -- except the order-n^3
+// metrics of the (+-1') classes when every metric eigenvalue is kept: there
+// the sums over the eigenpairs are resolvents of the pencil K v = w S v,
+// evaluated in its tridiagonal form without eigenvectors.  Energies
+// accumulate in FP64 on the device.
 #include <algorithm>
 #include <cmath>
 #include <cstring>

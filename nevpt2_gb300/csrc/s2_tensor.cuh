@@ -1,11 +1,14 @@
 // Device tensor toolkit for the NEVPT2 energy stage.
 //
 // Tensors are dense, C-ordered (last index fastest) FP64 arrays with up to 6
-// axes.  The stage-2 algebra is expressed with four primitives: an axis
+// axes.  The stage-2 algebra is expressed with a few primitives: an axis
 // permutation (materialised), the accessor builders of the reference's
 // qdnevpt-local normal-ordered products (src/qdnevpt.F:6448-6519), dense
-// GEMMs (cuBLAS) and symmetric eigendecompositions (cuSOLVER syevd).  All
-// work is enqueued on one stream; allocations are stream-ordered.
+// GEMMs (cuBLAS FP64, or split-precision digit products on the tensor cores
+// in split mode), symmetric eigendecompositions (cuSOLVER syevd) and, for
+// the order-n^3 pencils, Cholesky + reduction to standard form + the device
+// tridiagonalisation (tridiag.cu).  All work of one context is enqueued on
+// its stream; allocations are stream-ordered.
 #pragma once
 #include <cublas_v2.h>
 #include <cuda_runtime.h>
