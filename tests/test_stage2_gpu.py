@@ -1,7 +1,7 @@
 """Stage-2 CUDA path (nvpt_qdnevpt) against the oracle, per class.
 
-Tolerances: energies within 1e-9 Eh absolute (the FP64 bar of the north
-star); norms (dimensionless) within 1e-9 absolute or 1e-10 relative, since
+Tolerances: energies within 1e-9 Eh absolute (the FP64 parity bar of the
+path); norms (dimensionless) within 1e-9 absolute or 1e-10 relative, since
 near-singular PC denominators make them large; the PC metric ranks nnew are
 integers and must match exactly."""
 import numpy as np
