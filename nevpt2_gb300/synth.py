@@ -151,13 +151,17 @@ def fock_two_electron(L: np.ndarray, norb: int, ncore: int, nact: int, gamma1: n
     act = slice(ncore, ncore + nact)
     for q0 in range(0, Q, 64):
         B = _dense_B(L, norb, slice(q0, min(Q, q0 + 64)))
+        x = B.shape[0]
         Jc = np.einsum("xkk->x", B[:, :ncore, :ncore])
-        G += 2.0 * np.einsum("xpq,x->pq", B, Jc)
-        G -= np.einsum("xpk,xkq->pq", B[:, :, :ncore], B[:, :ncore, :])
         # gamma1[a,b] = <E_ab>; the reference multiplies (pq|ab) by da(b,a)
         Ja = np.einsum("xab,ba->x", B[:, act, act], gamma1)
-        G += np.einsum("xpq,x->pq", B, Ja)
-        G -= 0.5 * np.einsum("xpb,ba,xaq->pq", B[:, :, act], gamma1, B[:, act, :])
+        # Coulomb parts: sum_x B[x] (2 Jc[x] + Ja[x]) as one matrix-vector product
+        G += ((2.0 * Jc + Ja) @ B.reshape(x, norb * norb)).reshape(norb, norb)
+        # exchange parts as batched GEMMs: sum_x B[x][:, k] B[x][k, :] and B[x][:, act] gamma1 B[x][act, :]
+        Bk = np.ascontiguousarray(B[:, :, :ncore])
+        G -= np.matmul(Bk, np.ascontiguousarray(B[:, :ncore, :])).sum(axis=0)
+        Bg = np.matmul(np.ascontiguousarray(B[:, :, act]), gamma1)
+        G -= 0.5 * np.matmul(Bg, np.ascontiguousarray(B[:, act, :])).sum(axis=0)
     return G
 
 
