@@ -161,14 +161,15 @@ int nvpt_permute_3rdm_d(nvpt_context *ctx, double *rdm3, int64_t ld, int64_t nac
 
 /* Precision of the dense contractions of later calls on ctx (no counterpart
  * in the reference).  NVPT_PRECISION_FP64 (the default) is the drop-in.
- * NVPT_PRECISION_SPLIT runs the n^9 slab products of bamat as Ozaki digit
- * products on the tensor cores: each FP64 operand row/column is scaled by a
- * power of two, rounded to 60 bits and cut into ten 6-bit digits held
- * exactly in BF16, every digit pair with weight >= 2^-72 is summed exactly in
- * FP32, and the partial products are recombined in FP64 (error about 2^-61
- * of the row/column maximum per product).  Eigensolves, pseudo-inverses,
- * denominators and
- * energy sums always run in FP64. */
+ * NVPT_PRECISION_SPLIT runs the n^9 slab products of bamat, and in
+ * nvpt_qdnevpt the large products (DF integral blocks, metric and Koopmans
+ * builds, numerators), as Ozaki digit products on the tensor cores: each
+ * FP64 operand row/column is scaled by a power of two, rounded to 60 bits and
+ * cut into ten 6-bit digits held exactly in BF16, every digit pair with
+ * weight >= 2^-72 is summed exactly in FP32, and the partial products are
+ * recombined in integer and FP64 arithmetic (error about 2^-59..2^-61 of the
+ * row/column maximum per product).  Eigensolves, pseudo-inverses,
+ * triangular solves, denominators and energy sums always run in FP64. */
 #define NVPT_PRECISION_FP64 0
 #define NVPT_PRECISION_SPLIT 1
 int nvpt_set_precision(nvpt_context *ctx, int precision);
@@ -178,7 +179,8 @@ int nvpt_get_precision(nvpt_context *ctx);
  * (process-wide), tagged launches are bracketed by CUDA events on their
  * stream; nvpt_profile_read waits for and sums the spans of one tag (total
  * ms, launch count, algorithmic bytes) and forgets them.  Tags: "oz_gemm"
- * (the split-precision product kernel), "s2_prepare" (stage-2 orbitals and
+ * (the skinny split-precision product kernel), "oz_wide" (the general one;
+ * its bytes field holds the product's FP64 flops 2 m n k), "s2_prepare" (stage-2 orbitals and
  * transformed integrals of one state), "s2_class_0", "s2_class_+1",
  * "s2_class_-1", "s2_class_+2", "s2_class_-2", "s2_class_0p",
  * "s2_class_+1p", "s2_class_-1p" (one class of one state, on its stream). */
