@@ -87,3 +87,45 @@ def test_tridiagonal_solver_pivots():
     y = rng.standard_normal(n)
     x = _tridiag_solve(d, e, 0.0, y)
     assert np.abs(T @ x - y).max() <= 1e-10 * np.abs(T).max() * np.abs(x).max()
+
+
+def _to_band(A, b):
+    """Dense symmetric A -> band form of half-bandwidth b by block Householder
+    (two-sided QR of each panel below the band); returns the band matrix and
+    the panel transforms (row offset, orthogonal factor)."""
+    A = A.copy()
+    n = A.shape[0]
+    Qs = []
+    for k in range(0, n - b, b):
+        Qp, _ = np.linalg.qr(A[k + b:, k:k + b], mode="complete")
+        A[k + b:, :] = Qp.T @ A[k + b:, :]
+        A[:, k + b:] = A[:, k + b:] @ Qp
+        Qs.append((k + b, Qp))
+    return A, Qs
+
+
+def test_band_route_resolvents_equal_the_eigenpair_sums():
+    """The next step's route: resolvents on the band form (banded LU with
+    partial pivoting), no reduction to tridiagonal."""
+    rng = np.random.default_rng(11)
+    n, b = 150, 12
+    X = rng.standard_normal((n, n))
+    A = (X + X.T) / 2
+    Bm, Qs = _to_band(A, b)
+    assert np.abs(np.tril(Bm, -b - 1)).max() <= 1e-13 * np.abs(A).max()
+    w, V = np.linalg.eigh(A)
+    z = rng.standard_normal(n)
+    y = z.copy()
+    for k, Qp in Qs:
+        y[k:] = Qp.T @ y[k:]
+    for s in (0.3, -w[7] + 1e-6):
+        ref = np.sum((V.T @ z) ** 2 / (w + s))
+        M = Bm + s * np.eye(n)
+        ab = np.zeros((3 * b + 1, n))  # LAPACK general band storage with room for the pivoting fill
+        for j in range(n):
+            for i in range(max(0, j - b), min(n, j + b + 1)):
+                ab[2 * b + i - j, j] = M[i, j]
+        _, _, x, info = linalg.lapack.dgbsv(b, b, ab, y)
+        assert info == 0
+        cond = np.abs(w + s).max() / np.abs(w + s).min()
+        assert abs(y @ x - ref) <= 1e3 * np.finfo(float).eps * cond * np.sum(np.abs((V.T @ z) ** 2 / (w + s)))
