@@ -75,6 +75,20 @@ inline I mask_rank(uint32_t m, int n) {
 
 inline int popc(uint32_t x) { return __builtin_popcount(x); }
 
+// A zero-filled buffer whose pages are first touched by all threads (the
+// Gram blocks reach 1.7 GB at n = 16; a serial fill costs a second).
+struct ZeroBuf {
+    double *p;
+    explicit ZeroBuf(size_t count) : p(new double[count]) {
+#pragma omp parallel for schedule(static)
+        for (long long i = 0; i < (long long)count; ++i) p[i] = 0.0;
+    }
+    ~ZeroBuf() { delete[] p; }
+    ZeroBuf(const ZeroBuf &) = delete;
+    ZeroBuf &operator=(const ZeroBuf &) = delete;
+    double *data() { return p; }
+};
+
 struct Entry {
     uint64_t key;   // (xid << 24) | S
     int32_t det;    // +-(det+1): sign of the annihilation string
@@ -161,24 +175,58 @@ void gram_block(const Block &blk, I ndet, const uint32_t *amask, const uint32_t 
 #else
     std::sort(ent.begin(), ent.end(), [](const Entry &a, const Entry &b) { return a.key < b.key; });
 #endif
-    // groups by xid
+    // groups by xid (a group starts where xid changes), then the entries
+    // bucketed by S, ascending e inside a bucket, for a race-free,
+    // deterministic row-parallel update.  Both passes run over contiguous
+    // chunks of the entries: per-chunk counts, an exclusive scan over the
+    // chunks, then each chunk writes its own part -- the same arrays a
+    // sequential pass would produce.
     const I ne = (I)ent.size();
-    std::vector<I> gstart;
-    gstart.reserve(ne / 2 + 2);
-    std::vector<I> gid(ne);
-    for (I e = 0; e < ne; ++e) {
-        if (e == 0 || (ent[e].key >> 24) != (ent[e - 1].key >> 24)) gstart.push_back(e);
-        gid[e] = (I)gstart.size() - 1;
+    const int nch = std::max(1, std::min(256, (int)(ne / 65536) + 1));
+    auto chunk_lo = [&](int c) { return ne * c / nch; };
+    std::vector<I> heads(nch + 1, 0);
+#pragma omp parallel for schedule(static)
+    for (int c = 0; c < nch; ++c) {
+        I h = 0;
+        for (I e = chunk_lo(c); e < chunk_lo(c + 1); ++e)
+            if (e == 0 || (ent[e].key >> 24) != (ent[e - 1].key >> 24)) ++h;
+        heads[c + 1] = h;
     }
-    gstart.push_back(ne);
-    // bucket entries by S for a race-free, deterministic row-parallel update
-    std::vector<I> sstart(blk.dim + 1, 0);
-    for (I e = 0; e < ne; ++e) sstart[(ent[e].key & 0xFFFFFFull) + 1]++;
-    for (I q = 0; q < blk.dim; ++q) sstart[q + 1] += sstart[q];
+    for (int c = 0; c < nch; ++c) heads[c + 1] += heads[c];
+    std::vector<I> gstart((size_t)heads[nch] + 1);
+    std::vector<I> gid(ne);
+#pragma omp parallel for schedule(static)
+    for (int c = 0; c < nch; ++c) {
+        I g = heads[c] - 1;
+        for (I e = chunk_lo(c); e < chunk_lo(c + 1); ++e) {
+            if (e == 0 || (ent[e].key >> 24) != (ent[e - 1].key >> 24)) gstart[++g] = e;
+            gid[e] = g;
+        }
+    }
+    gstart[heads[nch]] = ne;
+    // counting sort by S: per-chunk histograms, bucket starts, chunk offsets
+    const I dim = blk.dim;
+    std::vector<I> hist((size_t)nch * dim, 0);
+#pragma omp parallel for schedule(static)
+    for (int c = 0; c < nch; ++c) {
+        I *hc = hist.data() + (size_t)c * dim;
+        for (I e = chunk_lo(c); e < chunk_lo(c + 1); ++e) hc[ent[e].key & 0xFFFFFFull]++;
+    }
+    std::vector<I> sstart(dim + 1, 0);
+    for (I q = 0; q < dim; ++q) {
+        I acc = sstart[q];
+        for (int c = 0; c < nch; ++c) {  // hist becomes each chunk's write offset in bucket q
+            const I h = hist[(size_t)c * dim + q];
+            hist[(size_t)c * dim + q] = acc;
+            acc += h;
+        }
+        sstart[q + 1] = acc;
+    }
     std::vector<I> sorder(ne);
-    {
-        std::vector<I> fill(sstart.begin(), sstart.end() - 1);
-        for (I e = 0; e < ne; ++e) sorder[fill[ent[e].key & 0xFFFFFFull]++] = e;
+#pragma omp parallel for schedule(static)
+    for (int c = 0; c < nch; ++c) {
+        I *off = hist.data() + (size_t)c * dim;
+        for (I e = chunk_lo(c); e < chunk_lo(c + 1); ++e) sorder[off[ent[e].key & 0xFFFFFFull]++] = e;
     }
     auto val = [&](I e, int root) {
         int32_t d = ent[e].det;
@@ -247,7 +295,7 @@ int rdmgen_dense(int n, int k, long ndet, const uint32_t *amask, const uint32_t 
     for (int i = 0; i < k; ++i) nk *= n;
     for (int r = 0; r <= k; ++r) {
         Block blk{n, k, r, BIN.t[n][r], BIN.t[n][k - r], BIN.t[n][r] * BIN.t[n][k - r]};
-        std::vector<double> D((size_t)(blk.dim * blk.dim), 0.0);
+        ZeroBuf D((size_t)(blk.dim * blk.dim));
         gram_block(blk, ndet, amask, bmask, coef, s, t, D.data());
         // (rank, sign) of every index tuple under every spin pattern of this block
         const unsigned nsp = 1u << k;
@@ -325,7 +373,7 @@ int rdmgen_ro4(int n, long ndet, const uint32_t *amask, const uint32_t *bmask, c
     std::vector<int8_t> tsg((size_t)16 * n4);
     for (int r = 0; r <= k; ++r) {
         Block blk{n, k, r, BIN.t[n][r], BIN.t[n][k - r], BIN.t[n][r] * BIN.t[n][k - r]};
-        std::vector<double> D((size_t)(blk.dim * blk.dim), 0.0);
+        ZeroBuf D((size_t)(blk.dim * blk.dim));
         gram_block(blk, ndet, amask, bmask, coef, s, s, D.data());
         // (rank, sign) of every L under every spin pattern of this block
 #pragma omp parallel for schedule(static)
