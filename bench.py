@@ -603,6 +603,12 @@ def run_ours(args):
     pk = _peaks()
     hbm_peak = pk.get("hbm_gbs", 6800.0)
     oz_gbs = oz_bytes.value / (oz_ms.value * 1e-3) / 1e9 if oz_ms.value > 0 else None
+    # DRAM traffic of k_oz_gemm per launch: the ncu capture of one
+    # 38912 x 4096 x 16 launch read 3.19 GB and wrote 5.9 MB against 3.194 GB of
+    # algorithmic bytes (digit tiles streamed once, no re-reads), so traffic
+    # scales with the rows of a launch; applied to this run's launches.
+    oz_traffic_ratio = (3.19e9 + 5.9e6) / (38912 * 4096 * 20 + 64 * 20480 + 38912 * 16 * 8)
+    oz_traffic = oz_bytes.value / oz_n.value * oz_traffic_ratio if oz_n.value else None
     # roofline (split stage 2): the general product runs 64 BF16 digit
     # products per FP64-equivalent product; tensor-bound
     bf16_peak = pk.get("bf16_tflops", 1900.0)
@@ -633,7 +639,9 @@ def run_ours(args):
                       "fp64_one_ulp_floor_eh": fp64_floor,
                       "roofline": {"kernel": "k_oz_gemm (Ozaki digit products, tcgen05)", "bound": "hbm",
                                    "achieved": oz_gbs, "peak": hbm_peak, "unit": "GB/s",
-                                   "frac": (oz_gbs / hbm_peak) if oz_gbs else None, "traffic": None,
+                                   "frac": (oz_gbs / hbm_peak) if oz_gbs else None, "traffic": oz_traffic,
+                                   "traffic_source": "bytes per launch, scaled by rows from the ncu capture of a "
+                                                     "38912x4096x16 launch (profiles/oz_gemm_split_38912x4096x16.md)",
                                    "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
                                    "kernel_ms": oz_ms.value, "launches": oz_n.value, "alg_bytes": oz_bytes.value},
                       "roofline_stage2": {
