@@ -59,6 +59,9 @@ def _args():
                     help="time the device tridiagonalisation of a symmetric matrix of order N and exit")
     ap.add_argument("--oz-wide", nargs=3, type=int, metavar=("M", "N", "K"),
                     help="time the general split-precision product C = A^T B (M x N, inner K) and exit")
+    ap.add_argument("--parity", action="store_true",
+                    help="compare the FP64 and split energies with the oracle's stage 2 fed the GPU's FP64 Koopmans "
+                         "matrices, per class and in total, with the split error split between stage 1 and stage 2")
     ap.add_argument("--oz-gemm", nargs=3, type=int, metavar=("ROWS", "K", "N"),
                     help="time the split-precision product kernel alone on a random ROWS x K by K x N problem")
     return ap.parse_args()
@@ -371,8 +374,8 @@ def energy_summary(e):
            "per_class_pc": [[float(x) for x in e.e2enp[:, s]] for s in range(M)],
            "nnew": [[int(x) for x in e.nnew[:, s]] for s in range(M)]}
     if M > 1:
-        out["qd_sc"] = [float(x) for x in gq.effective_hamiltonian(e.e2mp, np.zeros(M))[0]]
-        out["qd_pc"] = [float(x) for x in gq.effective_hamiltonian(e.e2en, np.zeros(M))[0]]
+        out["qd_sc"] = [float(x) for x in gq.effective_hamiltonian(e.e2mp, np.zeros(M)).wr]
+        out["qd_pc"] = [float(x) for x in gq.effective_hamiltonian(e.e2en, np.zeros(M)).wr]
     return out
 
 
@@ -641,7 +644,7 @@ def run_ours(args):
                                    "achieved": oz_gbs, "peak": hbm_peak, "unit": "GB/s",
                                    "frac": (oz_gbs / hbm_peak) if oz_gbs else None, "traffic": oz_traffic,
                                    "traffic_source": "bytes per launch, scaled by rows from the ncu capture of a "
-                                                     "38912x4096x16 launch (profiles/oz_gemm_split_38912x4096x16.md)",
+                                                     "38912x4096x16 launch (ncu: dram__bytes_read.sum + dram__bytes_write.sum)",
                                    "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
                                    "kernel_ms": oz_ms.value, "launches": oz_n.value, "alg_bytes": oz_bytes.value},
                       "roofline_stage2": {
@@ -661,6 +664,86 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_parity(args):
+    """Energies of the device path against the FP64 oracle on the benchmark
+    workload.  The oracle's stage 2 (numpy/LAPACK restatement of
+    src/qdnevpt.F) is fed the Koopmans matrices of the GPU's FP64 stage 1 (the
+    oracle's own n^9 bamat is out of reach at CAS(16,16); the tests compare it
+    with the GPU's on sampled slabs).  Reported, per class (max over states)
+    and for the SC/PC effective Hamiltonians: FP64 path - oracle, split path -
+    oracle, and the split error attributed to its two stages (split stage 1
+    with FP64 stage 2, FP64 stage 1 with split stage 2, each against the FP64
+    path), plus the PC metric ranks."""
+    import torch
+
+    from nevpt2_gb300 import koopro, synth
+    from nevpt2_gb300.pipeline import Stage1
+    from oracle import qdnevpt_oracle as q
+
+    dev = torch.device("cuda", 0)
+    t0 = time.perf_counter()
+    p = synth.config_problem(args.config)
+    t_gen = time.perf_counter() - t0
+    st = Stage1(p, device=str(dev))
+    ctx = st.ctx
+    stream = torch.cuda.Stream(dev)
+
+    def mode(m):
+        ctx.call("nvpt_set_precision", m)
+
+    def stage1(m):
+        mode(m)
+        with torch.cuda.stream(stream):
+            st.run(stream)
+        torch.cuda.synchronize(dev)
+
+    def stage2(m):
+        mode(m)
+        with torch.cuda.stream(stream):
+            e = st.stage2(stream)
+        torch.cuda.synchronize(dev)
+        return e
+
+    stage1(koopro.FP64)
+    e64 = stage2(koopro.FP64)
+    koop64 = {k: st.result(k) for k in st.out}
+    e_s2 = stage2(koopro.SPLIT)            # FP64 stage 1, split stage 2
+    stage1(koopro.SPLIT)
+    e_sp = stage2(koopro.SPLIT)            # split throughout
+    e_s1 = stage2(koopro.FP64)             # split stage 1, FP64 stage 2
+    mode(koopro.FP64)
+    koop = dict(koop64)
+    koop.update({"1-RDM": p.dal, "2-RDM": p.taa, "3-RDM": p.daaa})
+    t1 = time.perf_counter()
+    tr = None if p.trdm is None else tuple(list(t) for t in p.trdm)
+    ref = q.qdnevpt(q.inputs_from(p, koop, transition=tr))
+    t_orc = time.perf_counter() - t1
+
+    def diff(a, b):
+        pc = np.abs(np.asarray(a.e2enp) - np.asarray(b.e2enp))
+        sc = np.abs(np.asarray(a.e2mpp) - np.asarray(b.e2mpp))
+        return {"per_class_sc": [float(x) for x in sc.max(axis=1)], "per_class_pc": [float(x) for x in pc.max(axis=1)],
+                "total_sc": float(np.abs(np.asarray(a.e2mp) - np.asarray(b.e2mp)).max()),
+                "total_pc": float(np.abs(np.asarray(a.e2en) - np.asarray(b.e2en)).max())}
+
+    M = p.metat
+    keys = [(1, "p"), (2, "p"), (3, "a"), (3, "b"), (4, "a"), (4, "b"), (5, "p"), (6, "p"), (7, "p")]
+    nnew_ok = True
+    for s in range(M):
+        for slot, (cls, part) in enumerate(keys):
+            rk = (cls, s) if part == "p" else (cls, s, part)
+            if rk in ref.nnew and int(e64.nnew[slot, s]) != int(ref.nnew[rk]):
+                nnew_ok = False
+    out = {"parity": args.config, "workload": workload_desc(p)["workload"], "classes": q.CLASSES,
+           "fp64_vs_oracle_eh": diff(e64, ref), "split_vs_oracle_eh": diff(e_sp, ref),
+           "split_stage1_only_vs_fp64_eh": diff(e_s1, e64), "split_stage2_only_vs_fp64_eh": diff(e_s2, e64),
+           "nnew_fp64_equals_oracle": nnew_ok, "nnew_split_equals_fp64": bool(np.array_equal(e_sp.nnew, e64.nnew)),
+           "amat_split_vs_fp64_rel": float(max(np.abs(st.result(k) - koop64[k]).max() / np.abs(koop64[k]).max()
+                                              for k in ("amatIP", "amatEA"))),
+           "oracle_stage2_s": t_orc, "generator_s": t_gen}
+    print(json.dumps(out), flush=True)
+
+
 def live_ro4_entries(n: int) -> int:
     """Packed 4-RDM slots ord8 can address: (K sorted descending, L) with
     normind(L) <= normind(K)."""
@@ -678,7 +761,9 @@ def live_ro4_entries(n: int) -> int:
 
 if __name__ == "__main__":
     a = _args()
-    if a.sytrd:
+    if a.parity:
+        run_parity(a)
+    elif a.sytrd:
         run_sytrd(a)
     elif a.oz_wide:
         run_oz_wide(a)

@@ -222,8 +222,9 @@ int nvpt_sytrd_d(nvpt_context *ctx, int64_t n, double *A, double *d, double *e, 
  * pass is not acceptable.  All scratch is one file-scope device array sized
  * for nact <= 8 (4n^6 + 7n^4 + n^2 doubles at n = 8, 8.6 MB); larger nact
  * returns NVPT_EINVAL.  It calls no cudaMalloc/cudaFree and no allocating
- * library routine.  Its address is looked up once per device on the first
- * call, which must be made with the context's device current and should
+ * library routine.  Every call must be made with the context's device
+ * current (otherwise NVPT_EINVAL): the array has one address per device.
+ * That address is looked up on the first call on a device, which should
  * precede any stream capture.  No scratch word has to start at zero.  Calls
  * that overlap in time share the array and race: serialise them (one stream,
  * or events). */

@@ -8,7 +8,9 @@ source tree.  ``nvcc`` cross-compiles for sm_103a without a GPU.
 """
 from __future__ import annotations
 
+import hashlib
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -30,23 +32,47 @@ def _nvcc() -> str:
     return cand
 
 
-def _stale(target: Path, deps: list[Path]) -> bool:
-    if not target.exists():
+def _tool_version(tool: str) -> str:
+    r = subprocess.run([tool, "--version"], capture_output=True, text=True)
+    return r.stdout.strip()
+
+
+def _stamp(deps: list[Path], tool: str, flags: list[str]) -> str:
+    """What a library was built from: this machine's architecture and host
+    name, the compiler's version, the flags, and the sources' contents."""
+    h = hashlib.sha256()
+    for part in (platform.machine(), platform.node(), _tool_version(tool), " ".join(flags)):
+        h.update(part.encode() + b"\0")
+    for d in deps:
+        h.update(d.name.encode() + b"\0" + d.read_bytes())
+    return h.hexdigest()
+
+
+def _stale(target: Path, stamp: str) -> bool:
+    """A library is rebuilt unless it exists with a stamp file that matches:
+    a binary built elsewhere (another machine, compiler or source state) is
+    never reused."""
+    sfile = target.with_name(target.name + ".stamp")
+    if not target.exists() or not sfile.exists():
         return True
-    t = target.stat().st_mtime
-    return any(d.stat().st_mtime > t for d in deps)
+    return sfile.read_text().strip() != stamp
+
+
+def _write_stamp(target: Path, stamp: str) -> None:
+    target.with_name(target.name + ".stamp").write_text(stamp + "\n")
 
 
 def build_cuda(force: bool = False, verbose: bool = False) -> Path:
     out = PKG / "libnvpt2.so"
     deps = [CSRC / s for s in CUDA_SOURCES + CUDA_HEADERS] + [INCLUDE / "nvpt2.h"]
-    if not force and not _stale(out, deps):
-        return out
-    objdir = PKG / "_build"
-    objdir.mkdir(exist_ok=True)
     nvcc = _nvcc()
     flags = [GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
              f"-I{INCLUDE}", f"-I{CSRC}"]
+    stamp = _stamp(deps, nvcc, flags)
+    if not force and not _stale(out, stamp):
+        return out
+    objdir = PKG / "_build"
+    objdir.mkdir(exist_ok=True)
     procs = []
     objs = []
     for src in CUDA_SOURCES:
@@ -68,20 +94,37 @@ def build_cuda(force: bool = False, verbose: bool = False) -> Path:
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {r.stdout}\n{r.stderr}")
     os.replace(tmp, out)
+    _write_stamp(out, stamp)
     return out
 
 
 def build_rdmgen(force: bool = False) -> Path:
     out = PKG / "librdmgen.so"
     src = CSRC / "rdmgen.cpp"
-    if not force and not _stale(out, [src]):
+    flags = ["-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared"]
+    stamp = _stamp([src], "g++", flags)
+    if not force and not _stale(out, stamp):
         return out
     tmp = out.with_suffix(".so.tmp")
-    cmd = ["g++", "-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared", str(src), "-o", str(tmp)]
+    cmd = ["g++", *flags, str(src), "-o", str(tmp)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"g++ failed: {r.stdout}\n{r.stderr}")
     os.replace(tmp, out)
+    _write_stamp(out, stamp)
+    return out
+
+
+def build_oracle(force: bool = False) -> Path:
+    """The CPU oracle (test infrastructure, oracle/Makefile), rebuilt under
+    the same stamp rule as the product libraries."""
+    odir = PKG.parent / "oracle"
+    out = odir / "_build" / "liboracle.so"
+    stamp = _stamp([odir / "nvpt2_oracle.c", odir / "Makefile"], "gcc", [])
+    if not force and not _stale(out, stamp):
+        return out
+    subprocess.run(["make", "-s", "-B", "-C", str(odir)], check=True)
+    _write_stamp(out, stamp)
     return out
 
 

@@ -363,6 +363,27 @@ static int dgemm_rm(cublasHandle_t h, long long m, long long nn, long long k, co
                             &zero, C, (int)nn);
 }
 
+// Device buffers of one launch_bamat_gemm call, released on every return path
+// (stream-ordered frees on the call's stream).
+struct AsyncBuffers {
+    cudaStream_t st;
+    std::vector<void *> ptrs;
+    explicit AsyncBuffers(cudaStream_t s) : st(s) {}
+    template <class T>
+    bool get(T **p, size_t bytes) {
+        void *q = nullptr;
+        if (cudaMallocAsync(&q, bytes, st) != cudaSuccess) return false;
+        ptrs.push_back(q);
+        *p = (T *)q;
+        return true;
+    }
+    ~AsyncBuffers() {
+        for (auto it = ptrs.rbegin(); it != ptrs.rend(); ++it) cudaFreeAsync(*it, st);
+    }
+};
+
+__global__ void k_slab_list(int n, int *cp, int *ap);
+
 // Returns 0 on success, else a CUDA / cuBLAS error code (nonzero).
 int launch_bamat_gemm(const Rdm &r, const double *atwo, const double *f, int ncore, double *amat, double *atmat,
                       cudaStream_t st, int slabs_per_batch, bool split) {
@@ -374,44 +395,33 @@ int launch_bamat_gemm(const Rdm &r, const double *atwo, const double *f, int nco
     cublasSetMathMode(handle.h, CUBLAS_DEFAULT_MATH);
     // lower-order part first (writes amat/atmat), then add the GEMM terms
     {
+        AsyncBuffers rest(st);
         double *scr;
         const ll n2 = (ll)n * n;
-        if (cudaMallocAsync((void **)&scr, sizeof(double) * (4 * n6 + 5 * n4 + 4 * n2), st) != cudaSuccess) return 2;
+        if (!rest.get(&scr, sizeof(double) * (4 * n6 + 5 * n4 + 4 * n2))) return 2;
         int rrc = 0;
         for (int s = 0; s < M && !rrc; ++s) rrc = bamat_rest(handle.h, r, s, atwo, f, ncore, amat, atmat, scr, st);
-        cudaFreeAsync(scr, st);
         if (rrc) return 3;
     }
+    AsyncBuffers buf(st);
     double *A1, *A2, *A3, *T, *X;
     const int B = slabs_per_batch;
-    if (cudaMallocAsync((void **)&A1, sizeof(double) * 3 * n4, st) != cudaSuccess) return 2;
+    int *slabs;
+    if (!buf.get(&A1, sizeof(double) * 3 * n4) || !buf.get(&T, sizeof(double) * 4 * n6) ||
+        !buf.get(&X, sizeof(double) * 4 * (size_t)B * n6) || !buf.get(&slabs, sizeof(int) * 2 * n * n))
+        return 2;
     A2 = A1 + n4;
     A3 = A2 + n4;
     k_bamat_ints<<<(unsigned)((n4 + 255) / 256), 256, 0, st>>>(atwo, n, A1, A2, A3);
-    g_launches.fetch_add(1, std::memory_order_relaxed);
-    if (cudaMallocAsync((void **)&T, sizeof(double) * 4 * n6, st) != cudaSuccess) return 2;
-    if (cudaMallocAsync((void **)&X, sizeof(double) * 4 * (size_t)B * n6, st) != cudaSuccess) return 2;
-    int *slabs;
-    if (cudaMallocAsync((void **)&slabs, sizeof(int) * 2 * n * n, st) != cudaSuccess) return 2;
-    {
-        std::vector<int> h(2 * n * n);
-        for (int cp = 0; cp < n; ++cp)
-            for (int ap = 0; ap < n; ++ap) {
-                h[cp * n + ap] = cp;
-                h[n * n + cp * n + ap] = ap;
-            }
-        cudaMemcpyAsync(slabs, h.data(), sizeof(int) * 2 * n * n, cudaMemcpyHostToDevice, st);
-        cudaStreamSynchronize(st);
-    }
+    k_slab_list<<<(unsigned)((n * n + 255) / 256), 256, 0, st>>>(n, slabs, slabs + n * n);
+    g_launches.fetch_add(2, std::memory_order_relaxed);
     int rc = 0;
     // split precision: digit workspace for a full batch of slabs
     void *ozw = nullptr;
     unsigned long long *rmax = nullptr;  // row maxima of the four slab layouts (split digits)
     if (split) {
         oz::OzPlan pl(4, (ll)B * n3, (int)n3, n);
-        if (cudaMallocAsync(&ozw, pl.bytes(), st) != cudaSuccess) return 2;
-        if (cudaMallocAsync((void **)&rmax, sizeof(unsigned long long) * 4 * (size_t)B * n3, st) != cudaSuccess)
-            return 2;
+        if (!buf.get(&ozw, pl.bytes()) || !buf.get(&rmax, sizeof(unsigned long long) * 4 * (size_t)B * n3)) return 2;
     }
     for (int s = 0; s < M && !rc; ++s) {
         for (int s0 = 0; s0 < n * n && !rc; s0 += B) {
@@ -442,16 +452,8 @@ int launch_bamat_gemm(const Rdm &r, const double *atwo, const double *f, int nco
             g_launches.fetch_add(1, std::memory_order_relaxed);
         }
     }
-    if (ozw) {
-        // the product kernels share one error flag (a wait that timed out)
-        if (!rc && oz::oz_check_error(ozw, st) != 0) rc = 5;
-        cudaFreeAsync(ozw, st);
-        cudaFreeAsync(rmax, st);
-    }
-    cudaFreeAsync(slabs, st);
-    cudaFreeAsync(X, st);
-    cudaFreeAsync(T, st);
-    cudaFreeAsync(A1, st);
+    // the product kernels share one error flag (a wait that timed out)
+    if (ozw && !rc && oz::oz_check_error(ozw, st) != 0) rc = 5;
     return rc == 5 ? 5 : (rc ? 3 : 0);
 }
 
@@ -533,14 +535,16 @@ __global__ void k_bamat_assemble_slab(int n, int M, int s, int cp, int ap, const
 }
 
 double *bamat_static_scratch(int device) {
-    // One lookup per device, made with that device current (the caller's
-    // first call on it).
+    // The array's address differs per device, so every call checks that the
+    // context's device is the current one before it hands out an address
+    // (the cached address of another device would be a wild pointer here).
+    // The address is looked up once per device and cached.
     static std::atomic<double *> addr[64];
     if (device < 0 || device >= 64) return nullptr;
+    int cur = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess || cur != device) return nullptr;
     double *p = addr[device].load(std::memory_order_acquire);
     if (!p) {
-        int cur = -1;
-        if (cudaGetDevice(&cur) != cudaSuccess || cur != device) return nullptr;
         void *q = nullptr;
         if (cudaGetSymbolAddress(&q, g_bamat_scratch) != cudaSuccess) return nullptr;
         p = (double *)q;

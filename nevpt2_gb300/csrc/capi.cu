@@ -387,10 +387,12 @@ int nvpt_bamat_static_d(nvpt_context *ctx, double *amat, double *atmat, const do
                         std::to_string(kBamatStaticNactMax) + " active orbitals; use nvpt_bamat_d");
     if (nsym != 1) return fail(ctx, NVPT_ENOTSUP, "bamat: only the C1 (nsym=1) path is implemented");
     if (norb < ncore + nact) return fail(ctx, NVPT_EINVAL, "bamat: norb < ncore+nact");
+    int cur = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess || cur != ctx->device)
+        return fail(ctx, NVPT_EINVAL, "bamat_static: the context's device (" + std::to_string(ctx->device) +
+                                          ") must be the current device on every call");
     double *scr = bamat_static_scratch(ctx->device);
-    if (!scr)
-        return fail(ctx, NVPT_ECUDA, "bamat_static: scratch address lookup failed (the context's device must be "
-                                     "current on the first call)");
+    if (!scr) return fail(ctx, NVPT_ECUDA, "bamat_static: scratch address lookup failed");
     cudaStream_t st = pick(ctx, stream);
     Rdm r = make_rdm(nact, metat, dal, taa, daaa, ro4);
     launch_build_f(f, aj, atwo, (int)nact, (int)ncore, 1, st);

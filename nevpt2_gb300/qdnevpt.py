@@ -1,7 +1,8 @@
 """Host-side mirror of the reference's stage 2 (QDnevpt2.x): the per-state
 SC/PC-NEVPT2 loop of src/qdnevpt.F:858-993 on the GPU through
 ``nvpt_qdnevpt``, plus the metat x metat effective-Hamiltonian step of
-:1010-1230 (dgeev, ascending sort, Hermitisation) on the host.
+:1010-1230 (dgeev, ascending sort, and the Hermitisation of
+hermitian_heff, :8089-8183) on the host.
 
 Inputs use the nevpt.h5 dataset names and the reference's array shapes in
 numpy Fortran order (state index first).
@@ -111,11 +112,77 @@ def qdnevpt(problem, koop: dict, transition=None, thr_lindep: float = 1e-6, clas
     return res
 
 
-def effective_hamiltonian(e2: np.ndarray, energies: np.ndarray):
-    """src/qdnevpt.F:1046-1126: Heff = e2 + diag(E); eigenvalues of the
-    non-Hermitian matrix (dgeev), sorted ascending by real part.  Returns
-    (sorted eigenvalues (real parts), right eigenvectors, Heff)."""
-    H = np.array(e2, dtype=np.float64) + np.diag(energies)
-    w, vr = np.linalg.eig(H)
-    order = np.argsort(w.real, kind="stable")
-    return w.real[order], vr[:, order].real, H
+@dataclass
+class EffectiveHamiltonian:
+    """What src/qdnevpt.F:1046-1126 and hermitian_heff (:8089-8183) leave
+    behind for one of SC or PC.
+
+    heff       Heff = e2 + diag(E), the non-Hermitian matrix given to dgeev
+    wr, wi     its eigenvalues (real, imaginary parts), ascending in wr
+    vr, vl     right / left eigenvectors in dgeev's real storage, same order
+    heff_herm  the Hermitised Heff~ = C' diag(wr) C'^T with C' = vr S^-1/2 and
+               S = vr^T vr (the reference copies it back over e2mp / e2en)
+    evc_herm   eigenvectors of Heff~ (dsyev('V','U'), columns)
+    w_herm     eigenvalues of Heff~, ascending (stored in psimp / psien)
+    For one state (skip_effective_ham, src/qdnevpt.F:192) nothing is
+    diagonalised: heff_herm = heff, w_herm = its diagonal."""
+    heff: np.ndarray
+    wr: np.ndarray
+    wi: np.ndarray
+    vr: np.ndarray
+    vl: np.ndarray
+    heff_herm: np.ndarray
+    evc_herm: np.ndarray
+    w_herm: np.ndarray
+
+
+def _exchange_sort(wr, wi, vr, vl):
+    """The reference's reordering after dgeev (src/qdnevpt.F:1069-1089):
+    for i < j, swap eigenpairs i and j whenever wr(j) < wr(i)."""
+    wr, wi, vr, vl = wr.copy(), wi.copy(), vr.copy(), vl.copy()
+    m = wr.size
+    for i in range(m):
+        for j in range(i + 1, m):
+            if wr[j] < wr[i]:
+                wr[[i, j]] = wr[[j, i]]
+                wi[[i, j]] = wi[[j, i]]
+                vr[:, [i, j]] = vr[:, [j, i]]
+                vl[:, [i, j]] = vl[:, [j, i]]
+    return wr, wi, vr, vl
+
+
+def hermitian_heff(vr: np.ndarray, wr: np.ndarray):
+    """src/qdnevpt.F:8089-8183 (eq. 19 of JCP 121, 4043 (2004)): the
+    similarity transform that makes Heff Hermitian.  S = vr^T vr; S^-1/2 from
+    the eigenpairs of S (rtmatinv, :8305-8345); C' = vr S^-1/2;
+    Heff~ = C' diag(wr) C'^T; then Heff~ is diagonalised (dsyev('V','U')).
+    Returns (Heff~, its eigenvectors, its eigenvalues)."""
+    vr = np.asarray(vr, dtype=np.float64)
+    S = vr.T @ vr
+    ev, G = np.linalg.eigh(S, UPLO="U")
+    S_mhalf = (G / np.sqrt(ev)[None, :]) @ G.T
+    Cp = vr @ S_mhalf
+    H = (Cp * np.asarray(wr, dtype=np.float64)[None, :]) @ Cp.T
+    w, evc = np.linalg.eigh(H, UPLO="U")
+    return H, evc, w
+
+
+def effective_hamiltonian(e2: np.ndarray, energies: np.ndarray) -> EffectiveHamiltonian:
+    """src/qdnevpt.F:1046-1126 for one of SC (e2mp) or PC (e2en): add the
+    reference energies to the diagonal, diagonalise the non-Hermitian Heff
+    with LAPACK dgeev (left and right eigenvectors), reorder ascending by the
+    real parts as the reference does, and Hermitise (hermitian_heff)."""
+    from scipy.linalg import lapack
+
+    H = np.array(e2, dtype=np.float64) + np.diag(np.asarray(energies, dtype=np.float64))
+    m = H.shape[0]
+    if m == 1:
+        one = np.ones((1, 1))
+        return EffectiveHamiltonian(H, H.diagonal().copy(), np.zeros(1), one, one.copy(), H.copy(), one.copy(),
+                                    H.diagonal().copy())
+    wr, wi, vl, vr, info = lapack.dgeev(np.asfortranarray(H), compute_vl=1, compute_vr=1)
+    if info != 0:
+        raise RuntimeError(f"dgeev failed (info={info})")
+    wr, wi, vr, vl = _exchange_sort(wr, wi, vr, vl)
+    Hh, evc, w = hermitian_heff(vr, wr)
+    return EffectiveHamiltonian(H, wr, wi, vr, vl, Hh, evc, w)

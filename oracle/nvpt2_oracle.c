@@ -680,8 +680,74 @@ void orc_fdiff_F(const double *koopab, I nact, I metat, double *maxabs) {
 
 /* koopro4QD.F90:3974-4104 bamat, C1 branch.  The reference loops (a,b,c,ap,bp,cp)
  * and scatters the "transposed" EA terms into atmat(ap,b,cp,a,bp,c) under OpenMP
- * atomics; here the outer (a,c) pair is split across threads, which keeps every
- * write of one iteration inside the thread that owns (a,c). */
+ * atomics; here the (a,c) pair and ap are split across threads, which keeps every
+ * write of one iteration inside the thread that owns (a,c,ap).
+ * One (a,c) slab of the loop for one ap: every write of these iterations goes
+ * to an element whose (ap, a, c) indices are these, so (slab, ap) units are
+ * independent; within an element the contributions arrive in the reference's
+ * (b, bp, cp, d, ie, ief) order. */
+static void o_bamat_unit(const orc_ctx *cx, double *amat, double *atmat, const double *atwo, const double *f,
+                         I n, I ncore, I M, I slab, I ap) {
+    const I a = slab / n + 1, cc = slab % n + 1;
+            for (I b = 1; b <= n; ++b) {
+                    for (I bp = 1; bp <= n; ++bp)
+                        for (I cp = 1; cp <= n; ++cp)
+                            for (I d = 1; d <= n; ++d) {
+                                double fda = f[FIDX(d + ncore, a + ncore)];
+                                double fcd = f[FIDX(cc + ncore, d + ncore)];
+                                double fbd = f[FIDX(b + ncore, d + ncore)];
+                                for (I s = 1; s <= M; ++s) {
+                                    OUT7(amat, s, ap, bp, cp, a, b, cc) += fda * o_eee2(cx, cp, ap, bp, b, d, cc, s) -
+                                                                          fcd * o_eee2(cx, cp, ap, bp, b, a, d, s) -
+                                                                          fbd * o_eee2(cx, cp, ap, bp, d, a, cc, s);
+                                    OUT7(atmat, s, ap, bp, cp, a, b, cc) += fda * o_eee2t(cx, cp, ap, bp, b, d, cc, s) -
+                                                                           fcd * o_eee2t(cx, cp, ap, bp, b, a, d, s) +
+                                                                           fbd * o_eee2t(cx, cp, ap, bp, d, a, cc, s);
+                                }
+                                for (I ie = 1; ie <= n; ++ie) {
+                                    double dint1 = ATWO(cc, ie, d, a), dint2 = ATWO(d, ie, ie, a);
+                                    double dint3 = ATWO(cc, d, d, ie), dint4 = ATWO(b, d, d, ie);
+                                    for (I s = 1; s <= M; ++s) {
+                                        double dum1 = o_eee2(cx, cp, ap, bp, b, d, ie, s);
+                                        double dum2 = o_eee2(cx, cp, ap, bp, b, d, cc, s);
+                                        double dum3 = o_eee2(cx, cp, ap, bp, b, a, ie, s);
+                                        double dum4 = o_eee2(cx, cp, ap, bp, ie, a, cc, s);
+                                        double dum1t = -dum1, dum2t = -dum2, dum3t = -dum3;
+                                        if (bp == b) {
+                                            dum1t += 2.0 * o_ee2(cx, cp, ap, d, ie, s);
+                                            dum2t += 2.0 * o_ee2(cx, cp, ap, d, cc, s);
+                                            dum3t += 2.0 * o_ee2(cx, cp, ap, a, ie, s);
+                                        }
+                                        OUT7(atmat, s, ap, b, cp, a, bp, cc) += dum1t * dint1 - 0.5 * (dum2t * dint2 + dum3t * dint3);
+                                        double dum4t = o_eee2t(cx, cp, ap, bp, ie, a, cc, s);
+                                        OUT7(amat, s, ap, bp, cp, a, b, cc) += dum1 * dint1 - 0.5 * (dum2 * dint2 + dum3 * dint3 - dum4 * dint4);
+                                        OUT7(atmat, s, ap, bp, cp, a, b, cc) += 0.5 * dum4t * dint4;
+                                    }
+                                    for (I ief = 1; ief <= n; ++ief)
+                                        for (I s = 1; s <= M; ++s) {
+                                            double di1 = ATWO(d, ief, ie, a);
+                                            double e1 = o_eeee(cx, cp, ap, bp, b, d, ief, ie, cc, s);
+                                            double e1t = -e1;
+                                            if (bp == b) e1t += 2.0 * o_eee2(cx, cp, ap, d, ief, ie, cc, s);
+                                            OUT7(amat, s, ap, bp, cp, a, b, cc) += e1 * di1;
+                                            OUT7(atmat, s, ap, b, cp, a, bp, cc) += e1t * di1;
+                                            double e2 = o_eeee(cx, cp, ap, bp, b, d, ief, a, ie, s);
+                                            double e2t = -e2;
+                                            if (bp == b) e2t += 2.0 * o_eee2(cx, cp, ap, d, ief, a, ie, s);
+                                            double di2 = ATWO(d, ief, cc, ie);
+                                            OUT7(amat, s, ap, bp, cp, a, b, cc) -= e2 * di2;
+                                            OUT7(atmat, s, ap, b, cp, a, bp, cc) -= e2t * di2;
+                                            double e3 = o_eeee(cx, cp, ap, bp, ie, d, ief, a, cc, s);
+                                            double e3t = o_eeeet(cx, cp, ap, bp, ie, d, ief, a, cc, s);
+                                            double di3 = ATWO(d, ief, b, ie);
+                                            OUT7(amat, s, ap, bp, cp, a, b, cc) -= e3 * di3;
+                                            OUT7(atmat, s, ap, bp, cp, a, b, cc) += e3t * di3;
+                                        }
+                                }
+                            }
+            }
+}
+
 static void o_bamat_range(double *amat, double *atmat, const double *atwo, const double *ro4, const double *daaa,
                           const double *taa, const double *dal, I nact, I ncore, double *f, const double *aj,
                           I metat, I slab_lo, I slab_hi) {
@@ -690,67 +756,10 @@ static void o_bamat_range(double *amat, double *atmat, const double *atwo, const
     c.d1 = dal; c.d2 = taa; c.d3 = daaa; c.ro4 = ro4;
     I n = nact, M = metat;
     o_build_f(f, aj, atwo, n, ncore, 1);
+    const I units = (slab_hi - slab_lo) * n;
 #pragma omp parallel for schedule(dynamic, 1)
-    for (I slab = slab_lo; slab < slab_hi; ++slab)
-            for (I b = 1; b <= n; ++b) {
-                I a = slab / n + 1, cc = slab % n + 1;
-                for (I ap = 1; ap <= n; ++ap)
-                    for (I bp = 1; bp <= n; ++bp)
-                        for (I cp = 1; cp <= n; ++cp)
-                            for (I d = 1; d <= n; ++d) {
-                                double fda = f[FIDX(d + ncore, a + ncore)];
-                                double fcd = f[FIDX(cc + ncore, d + ncore)];
-                                double fbd = f[FIDX(b + ncore, d + ncore)];
-                                for (I s = 1; s <= M; ++s) {
-                                    OUT7(amat, s, ap, bp, cp, a, b, cc) += fda * o_eee2(&c, cp, ap, bp, b, d, cc, s) -
-                                                                          fcd * o_eee2(&c, cp, ap, bp, b, a, d, s) -
-                                                                          fbd * o_eee2(&c, cp, ap, bp, d, a, cc, s);
-                                    OUT7(atmat, s, ap, bp, cp, a, b, cc) += fda * o_eee2t(&c, cp, ap, bp, b, d, cc, s) -
-                                                                           fcd * o_eee2t(&c, cp, ap, bp, b, a, d, s) +
-                                                                           fbd * o_eee2t(&c, cp, ap, bp, d, a, cc, s);
-                                }
-                                for (I ie = 1; ie <= n; ++ie) {
-                                    double dint1 = ATWO(cc, ie, d, a), dint2 = ATWO(d, ie, ie, a);
-                                    double dint3 = ATWO(cc, d, d, ie), dint4 = ATWO(b, d, d, ie);
-                                    for (I s = 1; s <= M; ++s) {
-                                        double dum1 = o_eee2(&c, cp, ap, bp, b, d, ie, s);
-                                        double dum2 = o_eee2(&c, cp, ap, bp, b, d, cc, s);
-                                        double dum3 = o_eee2(&c, cp, ap, bp, b, a, ie, s);
-                                        double dum4 = o_eee2(&c, cp, ap, bp, ie, a, cc, s);
-                                        double dum1t = -dum1, dum2t = -dum2, dum3t = -dum3;
-                                        if (bp == b) {
-                                            dum1t += 2.0 * o_ee2(&c, cp, ap, d, ie, s);
-                                            dum2t += 2.0 * o_ee2(&c, cp, ap, d, cc, s);
-                                            dum3t += 2.0 * o_ee2(&c, cp, ap, a, ie, s);
-                                        }
-                                        OUT7(atmat, s, ap, b, cp, a, bp, cc) += dum1t * dint1 - 0.5 * (dum2t * dint2 + dum3t * dint3);
-                                        double dum4t = o_eee2t(&c, cp, ap, bp, ie, a, cc, s);
-                                        OUT7(amat, s, ap, bp, cp, a, b, cc) += dum1 * dint1 - 0.5 * (dum2 * dint2 + dum3 * dint3 - dum4 * dint4);
-                                        OUT7(atmat, s, ap, bp, cp, a, b, cc) += 0.5 * dum4t * dint4;
-                                    }
-                                    for (I ief = 1; ief <= n; ++ief)
-                                        for (I s = 1; s <= M; ++s) {
-                                            double di1 = ATWO(d, ief, ie, a);
-                                            double e1 = o_eeee(&c, cp, ap, bp, b, d, ief, ie, cc, s);
-                                            double e1t = -e1;
-                                            if (bp == b) e1t += 2.0 * o_eee2(&c, cp, ap, d, ief, ie, cc, s);
-                                            OUT7(amat, s, ap, bp, cp, a, b, cc) += e1 * di1;
-                                            OUT7(atmat, s, ap, b, cp, a, bp, cc) += e1t * di1;
-                                            double e2 = o_eeee(&c, cp, ap, bp, b, d, ief, a, ie, s);
-                                            double e2t = -e2;
-                                            if (bp == b) e2t += 2.0 * o_eee2(&c, cp, ap, d, ief, a, ie, s);
-                                            double di2 = ATWO(d, ief, cc, ie);
-                                            OUT7(amat, s, ap, bp, cp, a, b, cc) -= e2 * di2;
-                                            OUT7(atmat, s, ap, b, cp, a, bp, cc) -= e2t * di2;
-                                            double e3 = o_eeee(&c, cp, ap, bp, ie, d, ief, a, cc, s);
-                                            double e3t = o_eeeet(&c, cp, ap, bp, ie, d, ief, a, cc, s);
-                                            double di3 = ATWO(d, ief, b, ie);
-                                            OUT7(amat, s, ap, bp, cp, a, b, cc) -= e3 * di3;
-                                            OUT7(atmat, s, ap, bp, cp, a, b, cc) += e3t * di3;
-                                        }
-                                }
-                            }
-            }
+    for (I u = 0; u < units; ++u)
+        o_bamat_unit(&c, amat, atmat, atwo, f, n, ncore, M, slab_lo + u / n, u % n + 1);
     o_free(&c);
 }
 
@@ -769,6 +778,25 @@ void orc_bamat_slabs(double *amat, double *atmat, const double *atwo, const doub
                      I nslab) {
     if (nslab > nact * nact) nslab = nact * nact;
     o_bamat_range(amat, atmat, atwo, ro4, daaa, taa, dal, nact, ncore, f, aj, metat, 0, nslab);
+}
+
+/* bamat restricted to a list of (a,c) slabs (0-based slab = (a-1) n + (c-1)):
+ * the elements amat/atmat(s, ap, *, cp, a, *, c) of those slabs come out
+ * complete and exact, every other element stays as it was.  Used to check
+ * large active spaces on a sample of their outputs. */
+void orc_bamat_slab_list(double *amat, double *atmat, const double *atwo, const double *ro4, const double *daaa,
+                         const double *taa, const double *dal, I nact, I ncore, double *f, const double *aj,
+                         I metat, const I *slabs, I nslabs) {
+    orc_ctx c;
+    o_init(&c, nact, metat);
+    c.d1 = dal; c.d2 = taa; c.d3 = daaa; c.ro4 = ro4;
+    const I n = nact;
+    o_build_f(f, aj, atwo, n, ncore, 1);
+    const I units = nslabs * n;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (I u = 0; u < units; ++u)
+        o_bamat_unit(&c, amat, atmat, atwo, f, n, ncore, metat, slabs[u / n], u % n + 1);
+    o_free(&c);
 }
 
 /* koopro4QD.F90:4231-4299 bbmat (quirk: the EA part multiplies by aj, not f). */

@@ -45,6 +45,7 @@ def lib():
         L.orc_fdiff_F.argtypes = [P, I64, I64, P]
         L.orc_bamat.argtypes = [P] * 7 + [I64, I64, P, P, I64, I64]
         L.orc_bamat_slabs.argtypes = [P] * 7 + [I64, I64, P, P, I64, I64]
+        L.orc_bamat_slab_list.argtypes = [P] * 7 + [I64, I64, P, P, I64, P, I64]
         L.orc_bbmat.argtypes = [P] * 6 + [I64, I64, P, P, I64]
         L.orc_bcmat.argtypes = [P] * 6 + [I64, I64, P, P, I64]
         L.orc_bdmat.argtypes = [P] * 5 + [I64, I64, P, P, I64]
@@ -141,6 +142,27 @@ def bamat_slabs(atwo, ro4, daaa, taa, dal, nact, ncore, f, aj, metat, nslab):
     lib().orc_bamat_slabs(_p(amat), _p(atmat), _p(atwo), _p(ro4), _p(daaa), _p(taa), _p(dal), nact, ncore, _p(f),
                           _p(aj), metat, nslab)
     return amat, atmat
+
+
+def bamat_slab_list(atwo, ro4, daaa, taa, dal, nact, ncore, f, aj, metat, slabs):
+    """amat/atmat whose elements (s, ap, *, cp, a, *, c) are exact for the
+    0-based slabs (a-1) n + (c-1) listed; other elements are zero."""
+    amat, atmat = zeros(metat, *(nact,) * 6), zeros(metat, *(nact,) * 6)
+    sl = np.ascontiguousarray(slabs, dtype=np.int64)
+    lib().orc_bamat_slab_list(_p(amat), _p(atmat), _p(atwo), _p(ro4), _p(daaa), _p(taa), _p(dal), nact, ncore,
+                              _p(f), _p(aj), metat, _p(sl), sl.size)
+    return amat, atmat
+
+
+def slab_mask(nact, slabs):
+    """Boolean mask over (ap,bp,cp,a,b,c) (Fortran order, no state index) of
+    the elements the listed slabs determine."""
+    n = nact
+    m = np.zeros((n,) * 6, dtype=bool, order="F")
+    for sl in slabs:
+        a, c = divmod(int(sl), n)
+        m[:, :, :, a, :, c] = True
+    return m
 
 
 def bbmat(atwo, daaa, taa, dal, nact, ncore, f, aj, metat):

@@ -1162,3 +1162,44 @@ def inputs_from(problem, koop: dict, thr_lindep: float = 1e-6, transition=None) 
     if transition is not None:
         inp.daoff, inp.daaoff, inp.ro3off = transition
     return inp
+
+
+def heff_qd(e2, energies):
+    """src/qdnevpt.F:1050-1126 + hermitian_heff (:8089-8183) + rtmatinv
+    (:8305-8345), element loops as the reference writes them: Heff = e2 +
+    diag(E); dgeev('V','V'); exchange sort on wr; S_ij = <vr_i|vr_j>;
+    S^-1/2 = G diag(1/sqrt(eig)) G^T from dsyev('v','u'); C' = vr S^-1/2;
+    Heff~ = C' diag(wr) C'^T; dsyev('v','u') of Heff~.  Returns
+    (wr, wi, vr, Heff~, eigenvectors of Heff~, eigenvalues of Heff~)."""
+    H = np.array(e2, dtype=np.float64, order="F")
+    m = H.shape[0]
+    for i in range(m):
+        H[i, i] += energies[i]
+    wr, wi, vl, vr, info = sla.lapack.dgeev(H, compute_vl=1, compute_vr=1)
+    assert info == 0
+    for i in range(m):
+        for j in range(i + 1, m):
+            if wr[j] < wr[i]:
+                wr[i], wr[j] = wr[j], wr[i]
+                wi[i], wi[j] = wi[j], wi[i]
+                for k in range(m):
+                    vr[k, i], vr[k, j] = vr[k, j], vr[k, i]
+                    vl[k, i], vl[k, j] = vl[k, j], vl[k, i]
+    heff_evc = np.zeros((m, m), order="F")
+    for i in range(m):
+        heff_evc[i, i] = wr[i]
+    S = np.zeros((m, m), order="F")
+    for i in range(m):
+        for j in range(m):
+            S[i, j] = sum(vr[k, i] * vr[k, j] for k in range(m))
+    eig, G, info = sla.lapack.dsyev(S, compute_v=1, lower=0)
+    assert info == 0
+    D = np.zeros((m, m))
+    for i in range(m):
+        D[i, i] = 1.0 / np.sqrt(eig[i])
+    Smh = (G @ D) @ G.T
+    vr_tmp = vr @ Smh
+    Hh = (vr_tmp @ heff_evc) @ vr_tmp.T
+    w, evc, info = sla.lapack.dsyev(Hh, compute_v=1, lower=0)
+    assert info == 0
+    return wr, wi, vr, Hh, evc, w

@@ -73,9 +73,10 @@ def test_three_state_qd_and_heff(gpu_ctx):
     p = synth.make_problem(4, 4, 2, 3, metat=3, seed=9)
     ref, got = run_both(p)
     compare(ref, got)
-    w, v, H = gq.effective_hamiltonian(got.e2mp, np.zeros(3))
-    wr, _, _ = gq.effective_hamiltonian(ref.e2mp, np.zeros(3))
-    np.testing.assert_allclose(w, wr, rtol=0, atol=1e-9)
+    h = gq.effective_hamiltonian(got.e2mp, np.zeros(3))
+    hr = gq.effective_hamiltonian(ref.e2mp, np.zeros(3))
+    np.testing.assert_allclose(h.wr, hr.wr, rtol=0, atol=1e-9)
+    np.testing.assert_allclose(h.heff_herm, hr.heff_herm, rtol=0, atol=1e-9)
 
 
 def test_frozen_core_and_no_pc(gpu_ctx):
