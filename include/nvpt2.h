@@ -83,6 +83,36 @@ int nvpt_bro1(nvpt_context *ctx, const double *taa, double *dal, int64_t nact, i
 int nvpt_get_aj_atwo(nvpt_context *ctx, double *atwo, int64_t nact, int64_t ncore, int64_t norb, double *aj,
                      const double *oneint, const double *cholesky_array, int64_t nchovec);
 
+/* Symmetry-packed two-electron integrals (the non-Cholesky integral path of
+ * readint, src/ijkl_utils.F90:209-262, which supports point-group symmetry).
+ *
+ * nvpt_ijkl_init: src/infsym.F90:16 initialize_infsym (its = D2h product
+ * table, itsym = irrep of every orbital, inactive then active then secondary,
+ * irrep by irrep), src/ijkl_utils.F90:111 determine_n2int (ndeb, nad, kt,
+ * ni4) and :173 reijkl (num, indic, jndic), built on the device and kept in
+ * ctx.  nish/nash/nssh (nsym) are the inactive/active/secondary counts per
+ * irrep (inforb), nsym in {1,2,4,8}, norb = their sum <= 4096; *ni4
+ * receives the number of stored integrals (the length of twoint).
+ * nvpt_ijkl_tables: host copies of the tables (1-based values as in the
+ * reference): its (nsym,nsym), itsym (norb), num/indic/jndic
+ * (norb(norb+1)/2), ndeb (nsym), nad/kt (nsym(nsym+1)/2); NULL skips one.
+ * nvpt_ijkl_set_twoint: the integral list twoint(ni4) that ext2int2nev2int
+ * leaves in module state (src/ijkl_utils.F90:232-241), copied to the device.
+ * nvpt_ai_twoint: src/ijkl_utils.F90:690 ai_twoint for count quadruples
+ * (1-based, 4 per row); symmetry-forbidden integrals are 0.
+ * nvpt_get_aj_atwo_twoint: src/koopro4QD.F90:3900 get_aj_atwo with ai ->
+ * ai_twoint (src/ijkl_utils.F90:627); norb must be the one of init. */
+int nvpt_ijkl_init(nvpt_context *ctx, int64_t nsym, const int64_t *nish, const int64_t *nash, const int64_t *nssh,
+                   int64_t *ni4);
+int nvpt_ijkl_tables(nvpt_context *ctx, int64_t *its, int64_t *itsym, int64_t *num, int64_t *indic, int64_t *jndic,
+                     int64_t *ndeb, int64_t *nad, int64_t *kt);
+int nvpt_ijkl_set_twoint(nvpt_context *ctx, const double *twoint);
+int nvpt_ai_twoint(nvpt_context *ctx, int64_t count, const int64_t *ijkl, double *out);
+int nvpt_get_aj_atwo_twoint(nvpt_context *ctx, double *atwo, int64_t nact, int64_t ncore, int64_t norb, double *aj,
+                            const double *oneint);
+int nvpt_get_aj_atwo_twoint_d(nvpt_context *ctx, double *atwo, int64_t nact, int64_t ncore, int64_t norb, double *aj,
+                              const double *oneint, void *stream);
+
 /* src/koop_matrices.F90:16 koop_matrices_ctl(metat,nact,ncore,atwo,daaa,taa,dal,f,aj).
  * The reference writes its results to nevpt.h5; they are returned here in
  * the dataset shapes: ipko1/eako1 (metat,n,n) "1-IPKO"/"1-EAKO";

@@ -87,6 +87,12 @@ _SIGS = {
     "nvpt_bbmat_d": ([P] + [P] * 6 + [I64, I64, P, P, I64, P], ctypes.c_int),
     "nvpt_bcmat_d": ([P] + [P] * 6 + [I64, I64, P, P, I64, P], ctypes.c_int),
     "nvpt_bdmat_d": ([P] + [P] * 5 + [I64, I64, P, P, I64, P], ctypes.c_int),
+    "nvpt_ijkl_init": ([P, I64, P, P, P, P], ctypes.c_int),
+    "nvpt_ijkl_tables": ([P] + [P] * 8, ctypes.c_int),
+    "nvpt_ijkl_set_twoint": ([P, P], ctypes.c_int),
+    "nvpt_ai_twoint": ([P, I64, P, P], ctypes.c_int),
+    "nvpt_get_aj_atwo_twoint": ([P, P, I64, I64, I64, P, P], ctypes.c_int),
+    "nvpt_get_aj_atwo_twoint_d": ([P, P, I64, I64, I64, P, P, P], ctypes.c_int),
     # stage 2: struct pointers (nevpt2_gb300.qdnevpt rebinds them with typed structs)
     "nvpt_qdnevpt": ([P, P, P], ctypes.c_int),
     "nvpt_qdnevpt_d": ([P, P, P, P], ctypes.c_int),

@@ -348,6 +348,101 @@ __global__ void k_bamat_assemble(int n, int M, int s, const double *T1, const do
 }
 
 // ---------------------------------------------------------------------------
+// FP64 slab products.  Per slab batch the four contractions are row-major
+// C[rows, N] = X[rows, K] B[K, N] with K = n^3 and N = n <= 16: skinny
+// products whose cost is the FP64 pipe alone (2 FMA/clock/SM on GB300; the
+// 8 flops per X byte loaded are far above the HBM balance point), so the
+// kernel only has to keep that pipe busy.  One CTA computes a 128 x 16 tile
+// (columns beyond N are zero in shared memory and never stored); 256 threads,
+// each a 4 x 2 register block; X is staged 32 columns at a time, transposed in
+// shared memory (stride 129 doubles) so that a thread's four rows at one k are
+// contiguous, with the next chunk's global loads issued before the current
+// chunk's FMAs.  blockIdx.y selects one of up to four products.
+constexpr int kSkBM = 128, kSkBK = 32, kSkLd = kSkBM + 1;
+struct SkinnyJobs {
+    const double *X[4];
+    const double *B[4];
+    double *C[4];
+};
+
+__global__ void __launch_bounds__(256, 2) k_dgemm_skinny(SkinnyJobs jobs, ll rows, int N, int K) {
+    __shared__ double Xs[kSkBK * kSkLd];
+    __shared__ __align__(16) double Bs[kSkBK * 16];
+    // constant indices only (a dynamic index would copy the struct to local memory)
+    const int jb = blockIdx.y;
+    const double *__restrict__ X = jb == 0 ? jobs.X[0] : jb == 1 ? jobs.X[1] : jb == 2 ? jobs.X[2] : jobs.X[3];
+    const double *__restrict__ B = jb == 0 ? jobs.B[0] : jb == 1 ? jobs.B[1] : jb == 2 ? jobs.B[2] : jobs.B[3];
+    double *__restrict__ C = jb == 0 ? jobs.C[0] : jb == 1 ? jobs.C[1] : jb == 2 ? jobs.C[2] : jobs.C[3];
+    const int tid = threadIdx.x;
+    const ll r0 = (ll)blockIdx.x * kSkBM;
+    // loader mapping: lane = k within the chunk, warp = row (+ 8 i)
+    const int lk = tid & 31, lr = tid >> 5;
+    // compute mapping: 4 rows (tr*4..) x 2 columns (2 tc, 2 tc + 1)
+    const int tc = tid & 7, tr = tid >> 3;
+    double xr[16], br[2];
+    auto load = [&](int k0) {
+        const int k = k0 + lk;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const ll r = r0 + lr + 8 * i;
+            xr[i] = (r < rows && k < K) ? X[r * K + k] : 0.0;
+        }
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            const int e = tid + 256 * i, kk = e >> 4, c = e & 15;
+            br[i] = (c < N && k0 + kk < K) ? B[(ll)(k0 + kk) * N + c] : 0.0;
+        }
+    };
+    double acc[4][2] = {};
+    load(0);
+    for (int k0 = 0; k0 < K; k0 += kSkBK) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) Xs[lk * kSkLd + lr + 8 * i] = xr[i];
+#pragma unroll
+        for (int i = 0; i < 2; ++i) Bs[tid + 256 * i] = br[i];
+        __syncthreads();
+        if (k0 + kSkBK < K) load(k0 + kSkBK);
+#pragma unroll 8
+        for (int k = 0; k < kSkBK; ++k) {
+            const double *xs = Xs + k * kSkLd + tr * 4;
+            const double2 b = *reinterpret_cast<const double2 *>(Bs + k * 16 + 2 * tc);
+            const double x0 = xs[0], x1 = xs[1], x2 = xs[2], x3 = xs[3];
+            acc[0][0] = fma(x0, b.x, acc[0][0]);
+            acc[0][1] = fma(x0, b.y, acc[0][1]);
+            acc[1][0] = fma(x1, b.x, acc[1][0]);
+            acc[1][1] = fma(x1, b.y, acc[1][1]);
+            acc[2][0] = fma(x2, b.x, acc[2][0]);
+            acc[2][1] = fma(x2, b.y, acc[2][1]);
+            acc[3][0] = fma(x3, b.x, acc[3][0]);
+            acc[3][1] = fma(x3, b.y, acc[3][1]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const ll r = r0 + tr * 4 + i;
+        if (r >= rows) continue;
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+            if (2 * tc + j < N) C[r * N + 2 * tc + j] = acc[i][j];
+    }
+}
+
+static int dgemm_skinny4(cudaStream_t st, ll rows, int N, int K, const double *const X[4], const double *const B[4],
+                         double *const C[4]) {
+    SkinnyJobs j;
+    for (int i = 0; i < 4; ++i) {
+        j.X[i] = X[i];
+        j.B[i] = B[i];
+        j.C[i] = C[i];
+    }
+    dim3 grid((unsigned)((rows + kSkBM - 1) / kSkBM), 4);
+    k_dgemm_skinny<<<grid, 256, 0, st>>>(j, rows, N, K);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : 1;
+}
+
+// ---------------------------------------------------------------------------
 struct BamatGemm {
     cublasHandle_t h = nullptr;
     ~BamatGemm() {
@@ -441,10 +536,9 @@ int launch_bamat_gemm(const Rdm &r, const double *atwo, const double *f, int nco
                 rc |= oz::oz_gemm_skinny(oz::OzPlan(4, rows, (int)n3, n), Xs, As, Ts, n, n, ozw, st, Rm);
                 continue;
             }
-            rc |= dgemm_rm(handle.h, rows, n, n3, X1, A1, T1);
-            rc |= dgemm_rm(handle.h, rows, n, n3, X2, A2, T2);
-            rc |= dgemm_rm(handle.h, rows, n, n3, X3, A3, T3);
-            rc |= dgemm_rm(handle.h, rows, n, n3, X4, A3, T4);
+            const double *Xs[4] = {X1, X2, X3, X4}, *As[4] = {A1, A2, A3, A3};
+            double *Ts[4] = {T1, T2, T3, T4};
+            rc |= dgemm_skinny4(st, rows, n, (int)n3, Xs, As, Ts);
         }
         if (!rc) {
             k_bamat_assemble<<<(unsigned)((n6 + 255) / 256), 256, 0, st>>>(n, M, s, T, T + n6, T + 2 * n6, T + 3 * n6,

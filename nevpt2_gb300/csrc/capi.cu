@@ -91,12 +91,39 @@ void launch_ord8(const int64_t *in8, int64_t *out8, int64_t *lindex, long long c
 
 using namespace nvpt;
 
+// Device tables of the symmetry-packed integral path (nvpt_ijkl_init) and
+// the integral list (nvpt_ijkl_set_twoint), owned by the context.
+struct IjklState {
+    int nsym = 0, norb = 0;
+    long long ni4 = -1;
+    long long *tab = nullptr;  // its | itsym | num | indic | jndic | ndeb | nad | kt
+    double *twoint = nullptr;
+    long long npair() const { return (long long)norb * (norb + 1) / 2; }
+    long long *its() const { return tab; }
+    long long *itsym() const { return tab + nsym * nsym; }
+    long long *num() const { return itsym() + norb; }
+    long long *indic() const { return num() + npair(); }
+    long long *jndic() const { return indic() + npair(); }
+    long long *ndeb() const { return jndic() + npair(); }
+    long long *nad() const { return ndeb() + nsym; }
+    long long *kt() const { return nad() + nsym * (nsym + 1) / 2; }
+    long long total() const { return nsym * nsym + norb + 3 * npair() + nsym + nsym * (nsym + 1) + 2; }
+    void release() {
+        if (tab) cudaFree(tab);
+        if (twoint) cudaFree(twoint);
+        tab = nullptr;
+        twoint = nullptr;
+        ni4 = -1;
+    }
+};
+
 struct nvpt_context {
     int device = 0;
     int precision = NVPT_PRECISION_FP64;
     cudaStream_t stream = nullptr;
     std::string err;
     long long launches_at_create = 0;
+    IjklState ijkl;
 };
 
 namespace {
@@ -221,6 +248,7 @@ int nvpt_create(nvpt_context **out, int device) {
 int nvpt_destroy(nvpt_context *ctx) {
     if (!ctx) return NVPT_EINVAL;
     cudaStreamSynchronize(ctx->stream);
+    ctx->ijkl.release();
     cudaStreamDestroy(ctx->stream);
     delete ctx;
     return NVPT_OK;
@@ -334,6 +362,131 @@ int nvpt_get_aj_atwo_d(nvpt_context *ctx, double *atwo, int64_t nact, int64_t nc
     return after_launch(ctx, "get_aj_atwo");
 }
 
+// ------------------------------------------------ symmetry-packed integrals
+int nvpt_ijkl_init(nvpt_context *ctx, int64_t nsym, const int64_t *nish, const int64_t *nash, const int64_t *nssh,
+                   int64_t *ni4) {
+    if (!ctx) return NVPT_EINVAL;
+    if (!(nsym == 1 || nsym == 2 || nsym == 4 || nsym == 8))
+        return fail(ctx, NVPT_EINVAL, "ijkl_init: nsym must be 1, 2, 4 or 8 (a D2h subgroup)");
+    if (!nish || !nash || !nssh) return fail(ctx, NVPT_EINVAL, "ijkl_init: null orbital counts");
+    int64_t norb = 0;
+    for (int64_t r = 0; r < nsym; ++r) {
+        if (nish[r] < 0 || nash[r] < 0 || nssh[r] < 0) return fail(ctx, NVPT_EINVAL, "ijkl_init: negative count");
+        norb += nish[r] + nash[r] + nssh[r];
+    }
+    if (norb < 1 || norb > 4096) return fail(ctx, NVPT_EINVAL, "ijkl_init: norb must be in [1,4096]");
+    if (norb * (norb + 1) / 2 < nsym)
+        return fail(ctx, NVPT_EINVAL, "ijkl_init: norb(norb+1)/2 must be at least nsym (num is indexed by irrep)");
+    cudaStream_t st = ctx->stream;
+    ctx->ijkl.release();
+    IjklState &S = ctx->ijkl;
+    S.nsym = (int)nsym;
+    S.norb = (int)norb;
+    // tables + three count vectors + ni4 + the error flag
+    const size_t words = (size_t)S.total() + 3 * 8 + 2;
+    NV_TRY(cuda_check(ctx, cudaMalloc((void **)&S.tab, sizeof(long long) * words), "cudaMalloc (ijkl tables)"));
+    long long *cnt = S.tab + S.total(), *d_ni4 = cnt + 24;
+    int *bad = (int *)(d_ni4 + 1);
+    long long h[24] = {0};
+    for (int64_t r = 0; r < nsym; ++r) {
+        h[r] = nish[r];
+        h[8 + r] = nash[r];
+        h[16 + r] = nssh[r];
+    }
+    NV_TRY(cuda_check(ctx, cudaMemcpyAsync(cnt, h, sizeof(h), cudaMemcpyHostToDevice, st), "H2D copy"));
+    if (launch_ijkl_tables(S.nsym, cnt, cnt + 8, cnt + 16, S.norb, S.its(), S.itsym(), S.num(), S.indic(), S.jndic(),
+                           S.ndeb(), S.nad(), S.kt(), d_ni4, bad, st))
+        return after_launch(ctx, "ijkl_tables launch");
+    long long out[2] = {0, 0};
+    NV_TRY(cuda_check(ctx, cudaMemcpyAsync(out, d_ni4, sizeof(out), cudaMemcpyDeviceToHost, st), "D2H copy"));
+    NV_TRY(cuda_check(ctx, cudaStreamSynchronize(st), "ijkl_tables"));
+    if ((int)out[1] != 0) return fail(ctx, NVPT_EINVAL, "ijkl_init: orbital counts do not add up to norb");
+    S.ni4 = out[0];
+    if (ni4) *ni4 = S.ni4;
+    return NVPT_OK;
+}
+
+int nvpt_ijkl_tables(nvpt_context *ctx, int64_t *its, int64_t *itsym, int64_t *num, int64_t *indic, int64_t *jndic,
+                     int64_t *ndeb, int64_t *nad, int64_t *kt) {
+    if (!ctx) return NVPT_EINVAL;
+    const IjklState &S = ctx->ijkl;
+    if (S.ni4 < 0) return fail(ctx, NVPT_EINVAL, "ijkl_tables: call nvpt_ijkl_init first");
+    const long long np = S.npair(), nj = (long long)S.nsym * (S.nsym + 1) / 2;
+    struct { int64_t *h; const long long *d; long long n; } c[] = {
+        {its, S.its(), (long long)S.nsym * S.nsym}, {itsym, S.itsym(), S.norb}, {num, S.num(), np},
+        {indic, S.indic(), np}, {jndic, S.jndic(), np}, {ndeb, S.ndeb(), S.nsym}, {nad, S.nad(), nj},
+        {kt, S.kt(), nj}};
+    for (auto &x : c)
+        if (x.h)
+            NV_TRY(cuda_check(ctx, cudaMemcpyAsync(x.h, x.d, sizeof(int64_t) * x.n, cudaMemcpyDeviceToHost, ctx->stream),
+                              "D2H copy"));
+    return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "ijkl_tables");
+}
+
+int nvpt_ijkl_set_twoint(nvpt_context *ctx, const double *twoint) {
+    if (!ctx) return NVPT_EINVAL;
+    IjklState &S = ctx->ijkl;
+    if (S.ni4 < 0) return fail(ctx, NVPT_EINVAL, "ijkl_set_twoint: call nvpt_ijkl_init first");
+    if (!twoint) return fail(ctx, NVPT_EINVAL, "ijkl_set_twoint: null twoint");
+    if (!S.twoint)
+        NV_TRY(cuda_check(ctx, cudaMalloc((void **)&S.twoint, sizeof(double) * (size_t)(S.ni4 > 0 ? S.ni4 : 1)),
+                          "cudaMalloc (twoint)"));
+    NV_TRY(cuda_check(ctx, cudaMemcpyAsync(S.twoint, twoint, sizeof(double) * (size_t)S.ni4, cudaMemcpyHostToDevice,
+                                           ctx->stream), "H2D copy"));
+    return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "ijkl_set_twoint");
+}
+
+static int ijkl_ready(nvpt_context *ctx, const char *what, IjklTables *T) {
+    const IjklState &S = ctx->ijkl;
+    if (S.ni4 < 0 || !S.twoint)
+        return fail(ctx, NVPT_EINVAL, std::string(what) + ": call nvpt_ijkl_init and nvpt_ijkl_set_twoint first");
+    *T = IjklTables{S.num(), S.indic(), S.jndic(), S.ndeb(), S.nad(), S.kt(), S.twoint};
+    return NVPT_OK;
+}
+
+int nvpt_ai_twoint(nvpt_context *ctx, int64_t count, const int64_t *ijkl, double *out) {
+    if (!ctx) return NVPT_EINVAL;
+    IjklTables T;
+    NV_TRY(ijkl_ready(ctx, "ai_twoint", &T));
+    if (count < 0 || (count > 0 && (!ijkl || !out))) return fail(ctx, NVPT_EINVAL, "ai_twoint: bad buffers");
+    for (int64_t i = 0; i < 4 * count; ++i)
+        if (ijkl[i] < 1 || ijkl[i] > ctx->ijkl.norb) return fail(ctx, NVPT_EINVAL, "ai_twoint: index outside [1,norb]");
+    if (count == 0) return NVPT_OK;
+    Stage sg(ctx);
+    const int64_t *d_q = (const int64_t *)sg.up_bytes(ijkl, sizeof(int64_t) * 4 * (size_t)count);
+    double *d_o = sg.alloc(count);
+    NV_TRY(sg.status);
+    launch_ai_twoint(T, count, d_q, d_o, sg.st);
+    NV_TRY(after_launch(ctx, "ai_twoint"));
+    sg.down(out, d_o, count);
+    return sg.finish();
+}
+
+int nvpt_get_aj_atwo_twoint_d(nvpt_context *ctx, double *atwo, int64_t nact, int64_t ncore, int64_t norb, double *aj,
+                              const double *oneint, void *stream) {
+    NV_TRY(check_nact(ctx, nact, 1));
+    IjklTables T;
+    NV_TRY(ijkl_ready(ctx, "get_aj_atwo_twoint", &T));
+    if (ncore < 0 || norb != ctx->ijkl.norb || norb < ncore + nact)
+        return fail(ctx, NVPT_EINVAL, "get_aj_atwo_twoint: norb must be the one of nvpt_ijkl_init and >= ncore+nact");
+    launch_aj_atwo_twoint(T, oneint, (int)nact, (int)ncore, (int)norb, atwo, aj, pick(ctx, stream));
+    return after_launch(ctx, "get_aj_atwo_twoint");
+}
+
+int nvpt_get_aj_atwo_twoint(nvpt_context *ctx, double *atwo, int64_t nact, int64_t ncore, int64_t norb, double *aj,
+                            const double *oneint) {
+    NV_TRY(check_nact(ctx, nact, 1));
+    if (ncore < 0 || norb < ncore + nact) return fail(ctx, NVPT_EINVAL, "get_aj_atwo_twoint: bad sizes");
+    const int64_t npair = norb * (norb + 1) / 2;
+    Stage sg(ctx);
+    double *d_one = sg.up(oneint, npair), *d_aj = sg.alloc(npair), *d_atwo = sg.alloc(ipow(nact, 4));
+    NV_TRY(sg.status);
+    NV_TRY(nvpt_get_aj_atwo_twoint_d(ctx, d_atwo, nact, ncore, norb, d_aj, d_one, sg.st));
+    sg.down(atwo, d_atwo, ipow(nact, 4));
+    sg.down(aj, d_aj, npair);
+    return sg.finish();
+}
+
 int nvpt_koop_matrices_ctl_d(nvpt_context *ctx, int64_t metat, int64_t nact, int64_t ncore, const double *atwo,
                              const double *daaa, const double *taa, const double *dal, double *f, const double *aj,
                              double *ipko1, double *eako1, double *hrdm2, double *ipko2, double *eako2,
@@ -369,7 +522,7 @@ int nvpt_bamat_d(nvpt_context *ctx, double *amat, double *atmat, const double *a
         return after_launch(ctx, "bamat");
     }
     const bool split = ctx->precision == NVPT_PRECISION_SPLIT;
-    int slabs = split ? 16 : (nact >= 15 ? 2 : 4);
+    const int slabs = 16;
     int rc = launch_bamat_gemm(r, atwo, f, (int)ncore, amat, atmat, st, slabs, split);
     if (rc == 2) return fail(ctx, NVPT_ENOMEM, "bamat: device allocation failed");
     if (rc == 5) return fail(ctx, NVPT_ETIMEDOUT, "bamat: a split-precision product timed out waiting on its pipeline");

@@ -46,6 +46,18 @@ constexpr long long kBamatStaticDoubles = 4LL * 262144 + 7LL * 4096 + 64;  // 4n
 double *bamat_static_scratch(int device);
 int launch_bamat_static(const Rdm &r, const double *atwo, const double *f, int ncore, double *amat, double *atmat,
                         cudaStream_t st, double *scratch);
+// Symmetry-packed two-electron integrals (ijkl_sym.cu): device views of the
+// addressing tables of src/ijkl_utils.F90 (1-based values) and of twoint.
+struct IjklTables {
+    const long long *num, *indic, *jndic, *ndeb, *nad, *kt;
+    const double *twoint;
+};
+int launch_ijkl_tables(int nsym, const long long *nish, const long long *nash, const long long *nssh, int norb,
+                       long long *its, long long *itsym, long long *num, long long *indic, long long *jndic,
+                       long long *ndeb, long long *nad, long long *kt, long long *ni4, int *bad, cudaStream_t st);
+void launch_ai_twoint(const IjklTables &T, long long count, const int64_t *ijkl, double *out, cudaStream_t st);
+void launch_aj_atwo_twoint(const IjklTables &T, const double *oneint, int n, int ncore, int norb, double *atwo,
+                           double *aj, cudaStream_t st);
 // Kernel spans for live measurement (nvpt_set_profiling): when enabled, a
 // tagged launch is bracketed by CUDA events on its stream together with its
 // algorithmic byte count; nvpt_profile_read sums the spans of one tag.

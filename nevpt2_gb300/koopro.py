@@ -143,6 +143,56 @@ def bdmat(atwo, taa, dal, nact: int, ncore: int, f, aj, metat: int):
     return d, dt
 
 
+class SymmetryIntegrals:
+    """The non-Cholesky integral path with point-group symmetry
+    (src/ijkl_utils.F90:209-262 readint): the irrep and addressing tables of
+    initialize_infsym / determine_n2int / reijkl, built on the device by
+    ``nvpt_ijkl_init`` for the inactive/active/secondary counts per irrep,
+    and the symmetry-packed integral list ``twoint`` resident with them."""
+
+    KEYS = ("its", "itsym", "num", "indic", "jndic", "ndeb", "nad", "kt")
+
+    def __init__(self, nish, nash, nssh, ctx: Context | None = None):
+        self.ctx = ctx or context()
+        self.nsym = len(nish)
+        c = [np.ascontiguousarray(x, dtype=np.int64) for x in (nish, nash, nssh)]
+        ni4 = np.zeros(1, np.int64)
+        self.ctx.call("nvpt_ijkl_init", self.nsym, ptr(c[0]), ptr(c[1]), ptr(c[2]), ptr(ni4))
+        self.ni4 = int(ni4[0])
+        self.norb = int(sum(int(x.sum()) for x in c))
+
+    def tables(self) -> dict:
+        ns, no = self.nsym, self.norb
+        npair, nj = no * (no + 1) // 2, ns * (ns + 1) // 2
+        t = {"its": np.zeros((ns, ns), np.int64, order="F"), "itsym": np.zeros(no, np.int64),
+             "num": np.zeros(npair, np.int64), "indic": np.zeros(npair, np.int64),
+             "jndic": np.zeros(npair, np.int64), "ndeb": np.zeros(ns, np.int64), "nad": np.zeros(nj, np.int64),
+             "kt": np.zeros(nj, np.int64)}
+        self.ctx.call("nvpt_ijkl_tables", *[ptr(t[k]) for k in self.KEYS])
+        t["ni4"] = self.ni4
+        return t
+
+    def set_twoint(self, twoint) -> None:
+        tw = np.ascontiguousarray(twoint, dtype=np.float64)
+        if tw.size != self.ni4:
+            raise ValueError(f"twoint must hold ni4 = {self.ni4} integrals")
+        self.ctx.call("nvpt_ijkl_set_twoint", ptr(tw))
+
+    def ai(self, ijkl) -> np.ndarray:
+        """src/ijkl_utils.F90:690 ai_twoint for an (N,4) array of 1-based indices."""
+        q = np.ascontiguousarray(ijkl, dtype=np.int64).reshape(-1, 4)
+        out = np.zeros(q.shape[0])
+        self.ctx.call("nvpt_ai_twoint", q.shape[0], ptr(q), ptr(out))
+        return out
+
+    def get_aj_atwo(self, nact: int, ncore: int, oneint):
+        """src/koopro4QD.F90:3900 get_aj_atwo on this integral path."""
+        atwo = _z(nact, nact, nact, nact)
+        aj = np.zeros(self.norb * (self.norb + 1) // 2)
+        self.ctx.call("nvpt_get_aj_atwo_twoint", ptr(atwo), nact, ncore, self.norb, ptr(aj), ptr(_f(oneint)))
+        return atwo, aj
+
+
 def koopro4QD(problem) -> dict:
     """Stage 1 of one problem, in the reference driver's order
     (src/koopro4QD.F90:270-423): bro3/bro2/bro1 from the packed 4-RDM,

@@ -1129,3 +1129,119 @@ int orc_permute_3rdm(double *rdm3, I ld, I nact, const int32_t *labels, const do
 #undef DUMP3
     return bad;
 }
+
+/* ---------------------------------------------------------------------------
+ * Symmetry-packed two-electron integrals.
+ * infsym.F90:16-69 initialize_infsym (its, itsym), ijkl_utils.F90:111-170
+ * determine_n2int (ndeb, nad, kt, ni4), :173-207 reijkl (num, indic, jndic):
+ * sequential loops in the reference's order.  Arrays as in the reference,
+ * 1-based values: its (nsym,nsym), itsym (norb), num/indic/jndic (norb(norb+1)/2),
+ * ndeb (nsym), nad/kt (nsym(nsym+1)/2).  Returns ni4, or -1 if the counts do
+ * not add up to norb. */
+I orc_ijkl_tables(I nsym, const I *nish, const I *nash, const I *nssh, I norb, I *its, I *itsym, I *num, I *indic,
+                  I *jndic, I *ndeb, I *nad, I *kt) {
+    for (I i = 1; i <= nsym; ++i)
+        for (I j = 1; j <= nsym; ++j) its[(i - 1) + nsym * (j - 1)] = ((i - 1) ^ (j - 1)) + 1;
+    I k = 0;
+    const I *cnt[3] = {nish, nash, nssh};
+    for (int sp = 0; sp < 3; ++sp)
+        for (I i = 1; i <= nsym; ++i)
+            for (I j = 1; j <= cnt[sp][i - 1]; ++j) {
+                ++k;
+                if (k <= norb) itsym[k - 1] = i;
+            }
+    if (k != norb) return -1;
+    I nos[8] = {0};
+    /* reijkl: num(1) = 0, num(ij+1) = num(ij) + ij */
+    I ij = 0;
+    num[0] = 0;
+    for (I i = 2; i <= norb; ++i)
+        for (I j = 1; j <= i; ++j) {
+            ++ij;
+            num[ij] = num[ij - 1] + ij;
+        }
+    for (I i = 1; i <= norb; ++i) {
+        I is = itsym[i - 1];
+        for (I j = 1; j <= i; ++j) {
+            I js = itsym[j - 1];
+            I ijs = its[(is - 1) + nsym * (js - 1)];
+            nos[ijs - 1] += 1;
+            I p = num[i - 1] + j;
+            indic[p - 1] = ijs;
+            jndic[p - 1] = nos[ijs - 1];
+        }
+    }
+    /* determine_n2int: block offsets and the irrep-pair tables */
+    ndeb[0] = 0;
+    for (I r = 1; r <= nsym - 1; ++r) ndeb[r] = ndeb[r - 1] + nos[r - 1] * (nos[r - 1] + 1) / 2;
+    I ni4 = ndeb[nsym - 1] + nos[nsym - 1] * (nos[nsym - 1] + 1) / 2;
+    I njp = 0;
+    for (I is = 1; is <= nsym; ++is)
+        for (I js = 1; js <= is; ++js) {
+            ++njp;
+            if (js == is) {
+                nad[njp - 1] = is;
+                kt[njp - 1] = 1;
+            } else {
+                nad[njp - 1] = 0;
+                kt[njp - 1] = 0;
+            }
+        }
+    return ni4;
+}
+
+/* ijkl_utils.F90:690-756 ai_twoint (kt is 0 or 1 in these tables). */
+static double o_ai_twoint(const I *num, const I *indic, const I *jndic, const I *ndeb, const I *nad, const I *kt,
+                          const double *twoint, I i, I j, I k, I l) {
+    I ij = (i >= j) ? num[i - 1] + j : num[j - 1] + i;
+    I kl = (k >= l) ? num[k - 1] + l : num[l - 1] + k;
+    I ijs = indic[ij - 1], kls = indic[kl - 1], ijkls;
+    if (ijs <= kls) {
+        ijkls = num[kls - 1] + ijs;
+        I t = ij;
+        ij = kl;
+        kl = t;
+    } else {
+        ijkls = num[ijs - 1] + kls;
+    }
+    I nadv = nad[ijkls - 1];
+    if (nadv == 0) return 0.0;
+    int zsig = nadv < 0;
+    I nadi = zsig ? -nadv : nadv;
+    if (kt[ijkls - 1] != 1) return 0.0;
+    I nij = jndic[ij - 1], nkl = jndic[kl - 1];
+    I ijkl = (nij <= nkl) ? num[nkl - 1] + nij : num[nij - 1] + nkl;
+    double v = twoint[ndeb[nadi - 1] + ijkl - 1];
+    return zsig ? -v : v;
+}
+
+void orc_ai_twoint_list(const I *num, const I *indic, const I *jndic, const I *ndeb, const I *nad, const I *kt,
+                        const double *twoint, I count, const I *ijkl, double *out) {
+    for (I t = 0; t < count; ++t)
+        out[t] = o_ai_twoint(num, indic, jndic, ndeb, nad, kt, twoint, ijkl[4 * t], ijkl[4 * t + 1], ijkl[4 * t + 2],
+                             ijkl[4 * t + 3]);
+}
+
+/* koopro4QD.F90:3900-3971 get_aj_atwo with ai = ai_twoint. */
+void orc_get_aj_atwo_twoint(const I *num, const I *indic, const I *jndic, const I *ndeb, const I *nad, const I *kt,
+                            const double *twoint, const double *oneint, I nact, I ncore, I norb, double *atwo,
+                            double *aj) {
+    I n = nact;
+    memcpy(aj, oneint, sizeof(double) * (size_t)(norb * (norb + 1) / 2));
+#define AIT(a, b, c, d) o_ai_twoint(num, indic, jndic, ndeb, nad, kt, twoint, (a), (b), (c), (d))
+    for (I a = 1; a <= n; ++a) {
+        I ac = a + ncore;
+        for (I b = a; b <= n; ++b) {
+            I bc = b + ncore;
+            I jab = o_indice(ac, bc);
+            for (I j = 1; j <= ncore; ++j) aj[jab - 1] = aj[jab - 1] + 2.0 * AIT(ac, bc, j, j) - AIT(ac, j, j, bc);
+        }
+    }
+    for (I i = 1; i <= n; ++i)
+        for (I j = 1; j <= n; ++j)
+            for (I k = 1; k <= n; ++k)
+                for (I l = 1; l <= n; ++l)
+                    atwo[(i - 1) + n * ((j - 1) + n * ((k - 1) + n * (l - 1)))] =
+                        AIT(i + ncore, j + ncore, k + ncore, l + ncore);
+#undef AIT
+}

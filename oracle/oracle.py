@@ -53,6 +53,10 @@ def lib():
         L.orc_eeee_at.argtypes = [P, P, P, P, I64, I64, P, I64]; L.orc_eeee_at.restype = ctypes.c_double
         L.orc_eee2_at.argtypes = [P, P, P, I64, I64, P, I64]; L.orc_eee2_at.restype = ctypes.c_double
         L.orc_num_threads.restype = ctypes.c_int
+        L.orc_ijkl_tables.argtypes = [I64, P, P, P, I64] + [P] * 8
+        L.orc_ijkl_tables.restype = I64
+        L.orc_ai_twoint_list.argtypes = [P] * 7 + [I64, P, P]
+        L.orc_get_aj_atwo_twoint.argtypes = [P] * 8 + [I64, I64, I64, P, P]
         _lib = L
     return _lib
 
@@ -235,3 +239,79 @@ def permute_3rdm(flat, ld, n, labels, values, trans=False):
     bad = lib().orc_permute_3rdm(_p(flat), ld, n, _p(lab), _p(val), val.size, int(trans))
     return flat, bad
 
+
+
+# ---------------------------------------------------------------------------
+# Symmetry-packed two-electron integrals (infsym.F90, ijkl_utils.F90)
+
+def ijkl_tables(nish, nash, nssh):
+    """initialize_infsym + reijkl + determine_n2int: dict of the int64 tables
+    (1-based values) and ni4."""
+    nsym = len(nish)
+    norb = int(sum(nish) + sum(nash) + sum(nssh))
+    npair = norb * (norb + 1) // 2
+    c = [np.ascontiguousarray(x, dtype=np.int64) for x in (nish, nash, nssh)]
+    t = {"its": np.zeros((nsym, nsym), np.int64, order="F"), "itsym": np.zeros(norb, np.int64),
+         "num": np.zeros(npair, np.int64), "indic": np.zeros(npair, np.int64), "jndic": np.zeros(npair, np.int64),
+         "ndeb": np.zeros(nsym, np.int64), "nad": np.zeros(nsym * (nsym + 1) // 2, np.int64),
+         "kt": np.zeros(nsym * (nsym + 1) // 2, np.int64)}
+    ni4 = lib().orc_ijkl_tables(nsym, _p(c[0]), _p(c[1]), _p(c[2]), norb,
+                                *[_p(t[k]) for k in ("its", "itsym", "num", "indic", "jndic", "ndeb", "nad", "kt")])
+    t["ni4"] = int(ni4)
+    return t
+
+
+def _tab_ptrs(t, twoint):
+    return [_p(t[k]) for k in ("num", "indic", "jndic", "ndeb", "nad", "kt")] + [_p(twoint)]
+
+
+def ai_twoint(t, twoint, ijkl):
+    q = np.ascontiguousarray(ijkl, dtype=np.int64).reshape(-1, 4)
+    out = np.zeros(q.shape[0])
+    lib().orc_ai_twoint_list(*_tab_ptrs(t, twoint), q.shape[0], _p(q), _p(out))
+    return out
+
+
+def get_aj_atwo_twoint(t, twoint, oneint, nact, ncore, norb):
+    atwo = zeros(nact, nact, nact, nact)
+    aj = np.zeros(norb * (norb + 1) // 2)
+    lib().orc_get_aj_atwo_twoint(*_tab_ptrs(t, twoint), _p(np.ascontiguousarray(oneint)), nact, ncore, norb,
+                                 _p(atwo), _p(aj))
+    return atwo, aj
+
+
+def pack_twoint(t, chol):
+    """twoint in the reference's layout from a Cholesky/DF array whose
+    vectors respect the symmetry ((ij|kl) = sum_Q L[Q,ij] L[Q,kl] vanishes
+    unless indic(ij) == indic(kl)): per pair irrep r, the lower triangle of
+    the Gram matrix of its pairs (ranked by jndic), row by row, at ndeb(r)."""
+    L = np.asarray(chol)
+    tw = np.zeros(t["ni4"])
+    for r in range(1, len(t["ndeb"]) + 1):
+        pairs = np.nonzero(t["indic"] == r)[0]
+        pairs = pairs[np.argsort(t["jndic"][pairs])]
+        if pairs.size == 0:
+            continue
+        G = L[:, pairs].T @ L[:, pairs]
+        a, b = np.tril_indices(pairs.size)
+        tw[t["ndeb"][r - 1] + a * (a + 1) // 2 + b] = G[a, b]
+    return tw
+
+
+def symmetric_chol(itsym, nchovec, rng):
+    """A DF array L(Q, norb(norb+1)/2) with one irrep per vector: L[Q, pq] is
+    nonzero only when irrep(p) x irrep(q) equals vector Q's irrep (values
+    N(0, (0.05 exp(-|p-q|/8))^2) like the C1 generator)."""
+    itsym = np.asarray(itsym)
+    norb = itsym.size
+    nsym = int(itsym.max())
+    gq = rng.integers(0, nsym, nchovec)
+    L = np.zeros((nchovec, norb * (norb + 1) // 2), order="F")
+    col = 0
+    for p in range(norb):
+        for q in range(p + 1):
+            sd = 0.05 * np.exp(-abs(p - q) / 8.0)
+            pr = (itsym[p] - 1) ^ (itsym[q] - 1)
+            L[:, col] = np.where(gq == pr, rng.standard_normal(nchovec) * sd, 0.0)
+            col += 1
+    return L
