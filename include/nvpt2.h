@@ -217,6 +217,22 @@ int nvpt_get_precision(nvpt_context *ctx);
 int nvpt_set_profiling(nvpt_context *ctx, int on);
 int nvpt_profile_read(nvpt_context *ctx, const char *tag, double *ms, int64_t *launches, int64_t *bytes);
 
+/* Autotuning of launch parameters (no counterpart in the reference).  With
+ * on = 1, the first call that meets a new shape of a tuned kernel times
+ * every candidate of its parameter with CUDA events on the call's stream
+ * (synchronising that stream once) and keeps the fastest; later launches of
+ * that shape use the kept choice whether tuning is on or not (on = 0 stops
+ * tuning new shapes, on = 2 forgets every choice).  Tuned today: the tile
+ * height of the FP64 bamat slab products (64 or 128 rows) and the raster
+ * group of the general split-precision product (4 .. 32 row tiles sharing a
+ * column tile).  Candidates only reorder independent output tiles, so the
+ * results do not depend on the choice.  Choices are per device and shared by
+ * the contexts of a process.  nvpt_autotune_report writes them as JSON
+ * (choice and the timed milliseconds per candidate) into buf (len bytes,
+ * NUL-terminated) and returns the length the full text needs. */
+int nvpt_set_autotune(nvpt_context *ctx, int on);
+int64_t nvpt_autotune_report(nvpt_context *ctx, char *buf, int64_t len);
+
 /* The split-precision product as a building block (no counterpart in the
  * reference): row-major C[m,n] = A[m,k] B[k,n] on device pointers, with
  * n <= 16 and k <= 4096 (the exactness limit of the FP32 digit sums). */

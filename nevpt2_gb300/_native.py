@@ -87,6 +87,8 @@ _SIGS = {
     "nvpt_bbmat_d": ([P] + [P] * 6 + [I64, I64, P, P, I64, P], ctypes.c_int),
     "nvpt_bcmat_d": ([P] + [P] * 6 + [I64, I64, P, P, I64, P], ctypes.c_int),
     "nvpt_bdmat_d": ([P] + [P] * 5 + [I64, I64, P, P, I64, P], ctypes.c_int),
+    "nvpt_set_autotune": ([P, ctypes.c_int], ctypes.c_int),
+    "nvpt_autotune_report": ([P, ctypes.c_char_p, I64], I64),
     "nvpt_ijkl_init": ([P, I64, P, P, P, P], ctypes.c_int),
     "nvpt_ijkl_tables": ([P] + [P] * 8, ctypes.c_int),
     "nvpt_ijkl_set_twoint": ([P, P], ctypes.c_int),
@@ -145,6 +147,18 @@ class Context:
 
     def synchronize(self) -> None:
         self.call("nvpt_synchronize")
+
+    def autotune(self, on: bool = True) -> None:
+        """nvpt_set_autotune: tune the launch parameters of new shapes."""
+        self.call("nvpt_set_autotune", 1 if on else 0)
+
+    def autotune_report(self) -> dict:
+        """The tuned choices (nvpt_autotune_report) as a dict."""
+        import json
+        n = int(self._lib.nvpt_autotune_report(self.handle, None, 0))
+        buf = ctypes.create_string_buffer(n)
+        self._lib.nvpt_autotune_report(self.handle, buf, n)
+        return json.loads(buf.value.decode() or "{}")
 
     @property
     def launches(self) -> int:

@@ -21,6 +21,7 @@
 // corrections of eeee) in the four K-major layouts the GEMMs read.
 #include "nvpt2_internal.h"
 #include "ozaki.cuh"
+#include "tuner.h"
 
 #include <cublas_v2.h>
 
@@ -352,21 +353,24 @@ __global__ void k_bamat_assemble(int n, int M, int s, const double *T1, const do
 // C[rows, N] = X[rows, K] B[K, N] with K = n^3 and N = n <= 16: skinny
 // products whose cost is the FP64 pipe alone (2 FMA/clock/SM on GB300; the
 // 8 flops per X byte loaded are far above the HBM balance point), so the
-// kernel only has to keep that pipe busy.  One CTA computes a 128 x 16 tile
-// (columns beyond N are zero in shared memory and never stored); 256 threads,
-// each a 4 x 2 register block; X is staged 32 columns at a time, transposed in
-// shared memory (stride 129 doubles) so that a thread's four rows at one k are
-// contiguous, with the next chunk's global loads issued before the current
-// chunk's FMAs.  blockIdx.y selects one of up to four products.
-constexpr int kSkBM = 128, kSkBK = 32, kSkLd = kSkBM + 1;
+// kernel only has to keep that pipe busy.  One CTA computes a BM x 16 tile
+// (BM = 32 RPT; columns beyond N are zero in shared memory and never
+// stored); 256 threads, each an RPT x 2 register block; X is staged 32
+// columns at a time, transposed in shared memory (stride BM + 1 doubles) so
+// that a thread's rows at one k are contiguous, with the next chunk's global
+// loads issued before the current chunk's FMAs.  blockIdx.y selects one of up
+// to four products.  The tile height RPT is tuned per shape (tuner.h).
+constexpr int kSkBK = 32;
 struct SkinnyJobs {
     const double *X[4];
     const double *B[4];
     double *C[4];
 };
 
+template <int RPT>
 __global__ void __launch_bounds__(256, 2) k_dgemm_skinny(SkinnyJobs jobs, ll rows, int N, int K) {
-    __shared__ double Xs[kSkBK * kSkLd];
+    constexpr int BM = 32 * RPT, LD = BM + 1, NX = BM / 8;
+    __shared__ double Xs[kSkBK * LD];
     __shared__ __align__(16) double Bs[kSkBK * 16];
     // constant indices only (a dynamic index would copy the struct to local memory)
     const int jb = blockIdx.y;
@@ -374,16 +378,16 @@ __global__ void __launch_bounds__(256, 2) k_dgemm_skinny(SkinnyJobs jobs, ll row
     const double *__restrict__ B = jb == 0 ? jobs.B[0] : jb == 1 ? jobs.B[1] : jb == 2 ? jobs.B[2] : jobs.B[3];
     double *__restrict__ C = jb == 0 ? jobs.C[0] : jb == 1 ? jobs.C[1] : jb == 2 ? jobs.C[2] : jobs.C[3];
     const int tid = threadIdx.x;
-    const ll r0 = (ll)blockIdx.x * kSkBM;
+    const ll r0 = (ll)blockIdx.x * BM;
     // loader mapping: lane = k within the chunk, warp = row (+ 8 i)
     const int lk = tid & 31, lr = tid >> 5;
-    // compute mapping: 4 rows (tr*4..) x 2 columns (2 tc, 2 tc + 1)
+    // compute mapping: RPT rows (tr*RPT..) x 2 columns (2 tc, 2 tc + 1)
     const int tc = tid & 7, tr = tid >> 3;
-    double xr[16], br[2];
+    double xr[NX], br[2];
     auto load = [&](int k0) {
         const int k = k0 + lk;
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
+        for (int i = 0; i < NX; ++i) {
             const ll r = r0 + lr + 8 * i;
             xr[i] = (r < rows && k < K) ? X[r * K + k] : 0.0;
         }
@@ -393,39 +397,44 @@ __global__ void __launch_bounds__(256, 2) k_dgemm_skinny(SkinnyJobs jobs, ll row
             br[i] = (c < N && k0 + kk < K) ? B[(ll)(k0 + kk) * N + c] : 0.0;
         }
     };
-    double acc[4][2] = {};
+    double acc[RPT][2] = {};
     load(0);
     for (int k0 = 0; k0 < K; k0 += kSkBK) {
 #pragma unroll
-        for (int i = 0; i < 16; ++i) Xs[lk * kSkLd + lr + 8 * i] = xr[i];
+        for (int i = 0; i < NX; ++i) Xs[lk * LD + lr + 8 * i] = xr[i];
 #pragma unroll
         for (int i = 0; i < 2; ++i) Bs[tid + 256 * i] = br[i];
         __syncthreads();
         if (k0 + kSkBK < K) load(k0 + kSkBK);
 #pragma unroll 8
         for (int k = 0; k < kSkBK; ++k) {
-            const double *xs = Xs + k * kSkLd + tr * 4;
+            const double *xs = Xs + k * LD + tr * RPT;
             const double2 b = *reinterpret_cast<const double2 *>(Bs + k * 16 + 2 * tc);
-            const double x0 = xs[0], x1 = xs[1], x2 = xs[2], x3 = xs[3];
-            acc[0][0] = fma(x0, b.x, acc[0][0]);
-            acc[0][1] = fma(x0, b.y, acc[0][1]);
-            acc[1][0] = fma(x1, b.x, acc[1][0]);
-            acc[1][1] = fma(x1, b.y, acc[1][1]);
-            acc[2][0] = fma(x2, b.x, acc[2][0]);
-            acc[2][1] = fma(x2, b.y, acc[2][1]);
-            acc[3][0] = fma(x3, b.x, acc[3][0]);
-            acc[3][1] = fma(x3, b.y, acc[3][1]);
+#pragma unroll
+            for (int i = 0; i < RPT; ++i) {
+                const double x = xs[i];
+                acc[i][0] = fma(x, b.x, acc[i][0]);
+                acc[i][1] = fma(x, b.y, acc[i][1]);
+            }
         }
         __syncthreads();
     }
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const ll r = r0 + tr * 4 + i;
+    for (int i = 0; i < RPT; ++i) {
+        const ll r = r0 + tr * RPT + i;
         if (r >= rows) continue;
 #pragma unroll
         for (int j = 0; j < 2; ++j)
             if (2 * tc + j < N) C[r * N + 2 * tc + j] = acc[i][j];
     }
+}
+
+static void launch_skinny(int rpt, cudaStream_t st, const SkinnyJobs &j, ll rows, int N, int K) {
+    const ll bm = 32LL * rpt;
+    dim3 grid((unsigned)((rows + bm - 1) / bm), 4);
+    if (rpt == 2) k_dgemm_skinny<2><<<grid, 256, 0, st>>>(j, rows, N, K);
+    else k_dgemm_skinny<4><<<grid, 256, 0, st>>>(j, rows, N, K);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
 }
 
 static int dgemm_skinny4(cudaStream_t st, ll rows, int N, int K, const double *const X[4], const double *const B[4],
@@ -436,9 +445,13 @@ static int dgemm_skinny4(cudaStream_t st, ll rows, int N, int K, const double *c
         j.B[i] = B[i];
         j.C[i] = C[i];
     }
-    dim3 grid((unsigned)((rows + kSkBM - 1) / kSkBM), 4);
-    k_dgemm_skinny<<<grid, 256, 0, st>>>(j, rows, N, K);
-    g_launches.fetch_add(1, std::memory_order_relaxed);
+    // rows per thread (tile height 32 RPT), tuned per shape
+    static const int kRpt[] = {2, 4};
+    const std::string key = "bamat_skinny.rows_per_thread/" + std::to_string(rows) + "x" + std::to_string(K) + "x" +
+                            std::to_string(N);
+    int used = -1;
+    const int rpt = tune::choose(key, kRpt, 2, 4, st, [&](int c) { launch_skinny(c, st, j, rows, N, K); used = c; });
+    if (used < 0) launch_skinny(rpt, st, j, rows, N, K);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : 1;
 }
 

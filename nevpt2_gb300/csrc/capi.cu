@@ -1,6 +1,7 @@
 // C ABI of the library (include/nvpt2.h): context handling, argument checks,
 // host<->device staging for the drop-in host-pointer entry points, and the
 // device-pointer (_d) entry points that enqueue the kernels.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -12,6 +13,7 @@
 #include "../../include/nvpt2.h"
 #include "nvpt2_internal.h"
 #include "ozaki.cuh"
+#include "tuner.h"
 
 namespace nvpt {
 std::atomic<long long> g_launches{0};
@@ -282,6 +284,27 @@ const char *nvpt_context_error_set(nvpt_context *ctx, const char *msg) {
 void *nvpt_context_stream(nvpt_context *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
 
 int64_t nvpt_launch_count(const nvpt_context *ctx) { return ctx ? g_launches.load() - ctx->launches_at_create : 0; }
+
+int nvpt_set_autotune(nvpt_context *ctx, int on) {
+    if (!ctx) return NVPT_EINVAL;
+    if (on == 2) {
+        tune::clear();
+        return NVPT_OK;
+    }
+    tune::set_enabled(on != 0);
+    return NVPT_OK;
+}
+
+int64_t nvpt_autotune_report(nvpt_context *ctx, char *buf, int64_t len) {
+    if (!ctx) return -1;
+    const std::string r = tune::report();
+    if (buf && len > 0) {
+        const size_t k = std::min((size_t)(len - 1), r.size());
+        memcpy(buf, r.data(), k);
+        buf[k] = 0;
+    }
+    return (int64_t)r.size() + 1;
+}
 
 int64_t nvpt_nwords(int64_t nact) { return nact * (nact + 1) * (nact + 2) * (nact + 3) / 24; }
 

@@ -37,6 +37,7 @@
 #include "nvpt2_internal.h"
 #include "oz_ptx.cuh"
 #include "ozaki.cuh"
+#include "tuner.h"
 
 namespace nvpt {
 namespace oz {
@@ -49,7 +50,7 @@ constexpr int B_CHUNK = NSL * B_TILE;      // 40 KB
 constexpr int A_SLOTS = 8, B_SLOTS = 2;
 constexpr int NWT = TMAX + 1;              // weight blocks t = p + q
 constexpr int DRAIN_KC = 24;               // K chunks between drains (1536 columns)
-constexpr int GM = 16;                     // row tiles per raster group
+constexpr int GM_DEFAULT = 16;             // row tiles per raster group (tuned per shape)
 constexpr int W_THREADS = 32 * (EPI_WARPS + 2);
 constexpr int W_SMEM = A_SLOTS * A_TILE + B_SLOTS * B_CHUNK + 1024;
 static_assert(NWT * NT <= TMEM_COLS, "weight blocks fit TMEM");
@@ -104,16 +105,17 @@ struct WideArgs {
     long long ldc, m, n;
     int nrt, nct, nkc, lower, ctrans;
     double beta;
+    int gm;  // row tiles per raster group
 };
 
-// Tile t -> (row tile, column tile): groups of GM row tiles, column tiles
+// Tile t -> (row tile, column tile): groups of gm row tiles, column tiles
 // outer within a group, so consecutive CTAs share a column tile.
 __device__ __forceinline__ void tile_rc(const WideArgs &a, long long t, int &rt, int &ct) {
-    const long long per = (long long)GM * a.nct;
+    const long long per = (long long)a.gm * a.nct;
     const long long g = t / per, r = t % per;
-    const int rows_in = (int)min((long long)GM, (long long)a.nrt - g * GM);
+    const int rows_in = (int)min((long long)a.gm, (long long)a.nrt - g * a.gm);
     ct = (int)(r / rows_in);
-    rt = (int)(g * GM + r % rows_in);
+    rt = (int)(g * a.gm + r % rows_in);
 }
 // lower: skip tiles entirely above the diagonal (every column > every row)
 __device__ __forceinline__ bool tile_skip(const WideArgs &a, int rt, int ct) {
@@ -467,7 +469,7 @@ int oz_gemm_wide(const WideGemm &g, void *work, int *err, cudaStream_t st) {
         g.B, g.b_c, g.b_k, g.n, g.K, g.alpha, NT, L.nkc, cexp, bd);
     g_launches.fetch_add(4, std::memory_order_relaxed);
     WideArgs a{ad, bd, rexp, cexp, g.C, g.ldc, g.m, g.n, L.nrt, L.nct, L.nkc, g.lower ? 1 : 0, g.c_trans ? 1 : 0,
-               g.beta};
+               g.beta, GM_DEFAULT};
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -475,11 +477,27 @@ int oz_gemm_wide(const WideGemm &g, void *work, int *err, cudaStream_t st) {
     const unsigned grid = (unsigned)(tiles < sms ? tiles : sms);
     // recorded work: the FP64 flops of the product (2 m n K); the tensor
     // cores run 64 BF16 digit products of that size
-    ProfSpan span;
-    span.begin("oz_wide", st, 2 * g.m * g.n * (long long)g.K);
-    k_oz_wide<<<grid, W_THREADS, W_SMEM, st>>>(a, err);
-    span.end();
-    g_launches.fetch_add(1, std::memory_order_relaxed);
+    auto run = [&](int gm) {
+        a.gm = gm;
+        ProfSpan span;
+        span.begin("oz_wide", st, 2 * g.m * g.n * (long long)g.K);
+        k_oz_wide<<<grid, W_THREADS, W_SMEM, st>>>(a, err);
+        span.end();
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+    };
+    // raster group: tuned per shape when the product overwrites C (beta = 0:
+    // every trial writes the same result)
+    static const int kGm[] = {4, 8, 16, 32};
+    const std::string key = "oz_wide.raster_rows/" + std::to_string(L.nrt) + "x" + std::to_string(L.nct) + "x" +
+                            std::to_string(L.nkc) + (g.lower ? "L" : "");
+    const int cached = tune::lookup(key);
+    if (cached >= 0 || g.beta != 0.0) {
+        run(cached >= 0 ? cached : GM_DEFAULT);
+    } else {
+        int used = -1;
+        const int gm = tune::choose(key, kGm, 4, GM_DEFAULT, st, [&](int c) { run(c); used = c; });
+        if (used < 0) run(gm);  // tuning off: nothing launched yet
+    }
     return cudaGetLastError() == cudaSuccess ? 0 : 3;
 }
 

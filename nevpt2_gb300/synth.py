@@ -265,3 +265,26 @@ def config_problem(name: str, **over) -> Problem:
     kw.setdefault("with_trdm", kw["metat"] > 1)
     kw.update(over)
     return make_problem(**kw)
+
+
+BATCH_SEED = 20261203 * 100
+
+
+def batch_problems(count: int = 64, seed: int = BATCH_SEED, first: int = 0):
+    """The batched configuration: ``count`` independent problems, problem p
+    seeded with seed + p: active size uniform in {6, 8, 10, 12} at half
+    filling, 3 roots, inactive orbitals uniform in [5, 20], virtual orbitals
+    uniform in [30, 120], the full CAS space when it has at most 20,000
+    determinants (else 20,000 drawn uniformly: within the configuration's
+    bound of 100,000, and it keeps the host-side generator of 64 problems
+    within minutes), transition RDMs of the 3 root pairs."""
+    out = []
+    for pid in range(first, first + count):
+        r = np.random.default_rng(seed + pid)
+        n = int(r.choice([6, 8, 10, 12]))
+        nc = int(r.integers(5, 21))
+        nv = int(r.integers(30, 121))
+        full = math.comb(n, n // 2) ** 2
+        out.append(make_problem(n, n, nc, nv, metat=3, ndet=None if full <= 20_000 else 20_000, seed=seed + pid,
+                                with_trdm=True))
+    return out

