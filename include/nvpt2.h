@@ -36,6 +36,7 @@ extern "C" {
 #define NVPT_ENOMEM 3    /* device allocation failed                       */
 #define NVPT_ENOTSUP 4   /* configuration outside the supported path       */
 #define NVPT_ETIMEDOUT 5 /* a bounded device-side wait gave up             */
+#define NVPT_EIO 6       /* file missing, unreadable or not a container    */
 
 typedef struct nvpt_context nvpt_context;
 
@@ -188,6 +189,40 @@ int nvpt_permute_4rdm_d(nvpt_context *ctx, double *ro4, int64_t nact, const int3
                         int64_t nentries, void *stream);
 int nvpt_permute_3rdm_d(nvpt_context *ctx, double *rdm3, int64_t ld, int64_t nact, const int32_t *labels,
                         const double *values, int64_t nentries, int trans, void *stream);
+
+/* Dataset container for the path's files (no counterpart in the reference's
+ * code; it stands in for HDF5 where libhdf5 is absent).  Datasets keep the
+ * HDF5 names of the reference -- nevpt.h5 ("amatIP", "1-IPKO", "3-RDM", ...,
+ * src/koopro4QD.F90:305,369-418,473-477, src/qdnevpt.F:792-853) and the
+ * QCMaquis result datasets "/spectrum/results/fourptdm/labels_num" (int32,
+ * (8, nentries)) and ".../mean/value" (float64, (nentries)) -- with their
+ * element type (1 int32, 2 int64, 3 float64) and Fortran-order dims.
+ * nvpt_h5c_write creates the file (append = 0) or adds a dataset to it
+ * (append != 0; a later dataset of the same name replaces an earlier one);
+ * nvpt_h5c_info gives type, rank (<= 8) and dims; nvpt_h5c_read copies the
+ * payload (nbytes must match).  NVPT_EINVAL if the dataset is absent,
+ * NVPT_EIO if the file is missing or not a container. */
+int nvpt_h5c_write(const char *path, const char *name, int type, int rank, const int64_t *dims, const void *data,
+                   int append);
+int nvpt_h5c_info(const char *path, const char *name, int *type, int *rank, int64_t *dims);
+int nvpt_h5c_read(const char *path, const char *name, void *data, int64_t nbytes);
+/* Sorted names in a directory, newline-separated, into buf (len bytes);
+ * returns the length the full list needs, or -1 if dir cannot be opened. */
+int nvpt_h5c_list_dir(const char *path, char *buf, int64_t len);
+
+/* src/rdm_utils.F90:69 hdf5_read_rdm_from_resfile on a container file: the
+ * label/value lists of the 4-RDM (which = 4, into ro4(W,n,n,n,n) of one
+ * state, as nvpt_permute_4rdm) or the (transition, trans != 0) 3-RDM
+ * (which = 3, element stride ld, as nvpt_permute_3rdm); the reference's
+ * checks (8 or 6 labels per entry, label/value count match) give
+ * NVPT_EINVAL with its message.  *read_num_elements receives nentries. */
+int nvpt_read_rdm_from_resfile(nvpt_context *ctx, const char *path, int which, int trans, double *rdm, int64_t ld,
+                               int64_t nact, int64_t *read_num_elements);
+/* src/rdm_utils.F90:522 read_distributed_rdm: reads result_name from every
+ * subdirectory of dir that holds it, in sorted order, until total_elements
+ * entries have been read; fewer gives NVPT_EINVAL. */
+int nvpt_read_distributed_rdm(nvpt_context *ctx, const char *dir, const char *result_name, int which, int trans,
+                              double *rdm, int64_t ld, int64_t nact, int64_t total_elements);
 
 /* Precision of the dense contractions of later calls on ctx (no counterpart
  * in the reference).  NVPT_PRECISION_FP64 (the default) is the drop-in.

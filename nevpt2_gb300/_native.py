@@ -27,7 +27,7 @@ class NvptError(RuntimeError):
         self.status = status
 
 
-STATUS = {0: "NVPT_OK", 1: "NVPT_EINVAL", 2: "NVPT_ECUDA", 3: "NVPT_ENOMEM", 4: "NVPT_ENOTSUP", 5: "NVPT_ETIMEDOUT"}
+STATUS = {0: "NVPT_OK", 1: "NVPT_EINVAL", 2: "NVPT_ECUDA", 3: "NVPT_ENOMEM", 4: "NVPT_ENOTSUP", 5: "NVPT_ETIMEDOUT", 6: "NVPT_EIO"}
 
 
 def header_prototypes() -> dict[str, list[str]]:
@@ -89,6 +89,14 @@ _SIGS = {
     "nvpt_bdmat_d": ([P] + [P] * 5 + [I64, I64, P, P, I64, P], ctypes.c_int),
     "nvpt_set_autotune": ([P, ctypes.c_int], ctypes.c_int),
     "nvpt_autotune_report": ([P, ctypes.c_char_p, I64], I64),
+    "nvpt_h5c_write": ([ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int],
+                       ctypes.c_int),
+    "nvpt_h5c_info": ([ctypes.c_char_p, ctypes.c_char_p, P, P, P], ctypes.c_int),
+    "nvpt_h5c_read": ([ctypes.c_char_p, ctypes.c_char_p, P, I64], ctypes.c_int),
+    "nvpt_h5c_list_dir": ([ctypes.c_char_p, ctypes.c_char_p, I64], ctypes.c_int),
+    "nvpt_read_rdm_from_resfile": ([P, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, P, I64, I64, P], ctypes.c_int),
+    "nvpt_read_distributed_rdm": ([P, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, P, I64, I64,
+                                   I64], ctypes.c_int),
     "nvpt_ijkl_init": ([P, I64, P, P, P, P], ctypes.c_int),
     "nvpt_ijkl_tables": ([P] + [P] * 8, ctypes.c_int),
     "nvpt_ijkl_set_twoint": ([P, P], ctypes.c_int),

@@ -271,6 +271,7 @@ const char *nvpt_status_string(int status) {
         case NVPT_ENOMEM: return "device allocation failed";
         case NVPT_ENOTSUP: return "unsupported configuration";
         case NVPT_ETIMEDOUT: return "device wait timed out";
+        case NVPT_EIO: return "file error";
         default: return "unknown status";
     }
 }
