@@ -502,7 +502,8 @@ def run_ours(args):
     # device time of the stage-2 pieces in one FP64 step (spans on the pieces'
     # own streams; they overlap in time, so they do not add up to the step)
     S2_TAGS = ["s2_prepare", "s2_class_0", "s2_class_+1", "s2_class_-1", "s2_class_+2", "s2_class_-2",
-               "s2_class_0p", "s2_class_+1p", "s2_class_-1p"]
+               "s2_class_0p", "s2_class_+1p", "s2_class_-1p", "pencil_potrf", "pencil_reduce", "pencil_sytrd",
+               "pencil_rhs", "pencil_solve"]
 
     def stage2_breakdown():
         ctx.call("nvpt_set_profiling", 1)

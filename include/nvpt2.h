@@ -126,7 +126,15 @@ int nvpt_koop_matrices_ctl(nvpt_context *ctx, int64_t metat, int64_t nact, int64
                            double *gk0pd, double *gk0pf);
 
 /* src/koopro4QD.F90:3974 bamat(amat,atmat,atwo,ro4,daaa,taa,dal,nact,ncore,f,aj,norb,metat,nsym):
- * amat "amatIP", atmat "amatEA", both (metat,n^6).  nsym must be 1. */
+ * amat "amatIP", atmat "amatEA", both (metat,n^6).  nsym = 1 is the C1
+ * branch (:4008-4104).  nsym > 1 is the symmetry-screened branch
+ * (:4105-4228): it needs nvpt_ijkl_init on ctx with the same nsym and norb
+ * (the orbital irreps), computes the same dense contractions -- the terms the
+ * reference skips carry integrals that vanish by symmetry -- and zeroes the
+ * elements the reference never assigns (irreps of ap,bp,cp,a,b,c not
+ * multiplying to the totally symmetric one).  With symmetry tables on ctx,
+ * nvpt_koop_matrices_ctl likewise applies koop2E's screen
+ * (src/koop_matrices.F90:289-351) to the 2-IP/2-EA matrices. */
 int nvpt_bamat(nvpt_context *ctx, double *amat, double *atmat, const double *atwo, const double *ro4,
                const double *daaa, const double *taa, const double *dal, int64_t nact, int64_t ncore, double *f,
                const double *aj, int64_t norb, int64_t metat, int64_t nsym);
@@ -248,7 +256,11 @@ int nvpt_get_precision(nvpt_context *ctx);
  * its bytes field holds the product's FP64 flops 2 m n k), "s2_prepare" (stage-2 orbitals and
  * transformed integrals of one state), "s2_class_0", "s2_class_+1",
  * "s2_class_-1", "s2_class_+2", "s2_class_-2", "s2_class_0p",
- * "s2_class_+1p", "s2_class_-1p" (one class of one state, on its stream). */
+ * "s2_class_+1p", "s2_class_-1p" (one class of one state, on its stream);
+ * "pencil_potrf", "pencil_reduce", "pencil_sytrd", "pencil_rhs",
+ * "pencil_solve" (the steps of one order-n^3 PC pencil: metric Cholesky,
+ * reduction to standard form, tridiagonalisation, right-hand sides and the
+ * per-label tridiagonal solves). */
 int nvpt_set_profiling(nvpt_context *ctx, int on);
 int nvpt_profile_read(nvpt_context *ctx, const char *tag, double *ms, int64_t *launches, int64_t *bytes);
 

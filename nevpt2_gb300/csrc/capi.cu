@@ -525,6 +525,9 @@ int nvpt_koop_matrices_ctl_d(nvpt_context *ctx, int64_t metat, int64_t nact, int
     launch_hrdm(r, hrdm2, st);
     launch_build_f(f, aj, atwo, n, nc, 1, st);
     launch_koop2E(r, atwo, f, nc, ipko2, eako2, st);
+    // koop2E's its() screen with the context's symmetry tables (none: C1)
+    if (ctx->ijkl.ni4 >= 0 && ctx->ijkl.nsym > 1 && ctx->ijkl.norb >= ncore + nact)
+        launch_sym_screen(ipko2, eako2, (int)metat, n, 4, ctx->ijkl.itsym() + ncore, st);
     launch_koop0p(r, atwo, f, nc, gk0pa, gk0pd, gk0pf, st);
     return after_launch(ctx, "koop_matrices_ctl");
 }
@@ -533,16 +536,27 @@ int nvpt_bamat_d(nvpt_context *ctx, double *amat, double *atmat, const double *a
                  const double *daaa, const double *taa, const double *dal, int64_t nact, int64_t ncore, double *f,
                  const double *aj, int64_t norb, int64_t metat, int64_t nsym, void *stream) {
     NV_TRY(check_nact(ctx, nact, metat));
-    if (nsym != 1) return fail(ctx, NVPT_ENOTSUP, "bamat: only the C1 (nsym=1) path is implemented");
     if (norb < ncore + nact) return fail(ctx, NVPT_EINVAL, "bamat: norb < ncore+nact");
+    const long long *irr = nullptr;
+    if (nsym != 1) {
+        // the symmetry-screened branch: the irreps come from the context's
+        // integral tables (nvpt_ijkl_init), the reference's module state
+        const IjklState &S = ctx->ijkl;
+        if (S.ni4 < 0 || S.nsym != nsym || S.norb != norb)
+            return fail(ctx, NVPT_ENOTSUP, "bamat: nsym > 1 needs nvpt_ijkl_init with the same nsym and norb");
+        irr = S.itsym() + ncore;
+    }
     cudaStream_t st = pick(ctx, stream);
     Rdm r = make_rdm(nact, metat, dal, taa, daaa, ro4);
     launch_build_f(f, aj, atwo, (int)nact, (int)ncore, 1, st);
     // Tiny active spaces: one thread per element evaluates the reference's
     // loop directly.  Otherwise the n^9 part runs as dense GEMMs over
-    // materialised four-operator slabs (bamat_gemm.cu).
+    // materialised four-operator slabs (bamat_gemm.cu).  With symmetry the
+    // dense contractions are the same (the integrals the reference's branch
+    // skips vanish by symmetry) and its output screen follows.
     if (nact <= 5) {
         launch_bamat_direct(r, atwo, f, (int)ncore, amat, atmat, st);
+        if (irr) launch_sym_screen(amat, atmat, (int)metat, (int)nact, 6, irr, st);
         return after_launch(ctx, "bamat");
     }
     const bool split = ctx->precision == NVPT_PRECISION_SPLIT;
@@ -550,7 +564,8 @@ int nvpt_bamat_d(nvpt_context *ctx, double *amat, double *atmat, const double *a
     int rc = launch_bamat_gemm(r, atwo, f, (int)ncore, amat, atmat, st, slabs, split);
     if (rc == 2) return fail(ctx, NVPT_ENOMEM, "bamat: device allocation failed");
     if (rc == 5) return fail(ctx, NVPT_ETIMEDOUT, "bamat: a split-precision product timed out waiting on its pipeline");
-    if (rc) return fail(ctx, NVPT_ECUDA, split ? "bamat: split-precision product failed" : "bamat: cuBLAS GEMM failed");
+    if (rc) return fail(ctx, NVPT_ECUDA, split ? "bamat: split-precision product failed" : "bamat: GEMM failed");
+    if (irr) launch_sym_screen(amat, atmat, (int)metat, (int)nact, 6, irr, st);
     return after_launch(ctx, "bamat");
 }
 
@@ -834,7 +849,6 @@ int nvpt_bamat(nvpt_context *ctx, double *amat, double *atmat, const double *atw
                const double *daaa, const double *taa, const double *dal, int64_t nact, int64_t ncore, double *f,
                const double *aj, int64_t norb, int64_t metat, int64_t nsym) {
     NV_TRY(check_nact(ctx, nact, metat));
-    if (nsym != 1) return fail(ctx, NVPT_ENOTSUP, "bamat: only the C1 (nsym=1) path is implemented");
     int64_t M = metat, n2 = ipow(nact, 2), n4 = ipow(nact, 4), n6 = ipow(nact, 6), nf = f_len(nact, ncore);
     int64_t W = nvpt_nwords(nact);
     Stage S(ctx);

@@ -154,6 +154,36 @@ __global__ void k_aj_twoint(IjklTables T, const double *oneint, int n, int ncore
     aj[jab] = v;
 }
 
+// Output screens of the symmetry branches: an element whose orbitals'
+// irreps multiply to a non-symmetric irrep is set to zero -- bamat's
+// isatot /= 1 (src/koopro4QD.F90:4105-4133: all six indices of
+// amat/atmat(s,ap,bp,cp,a,b,c)) and koop2E's its(isab,iscd) /= 1
+// (src/koop_matrices.F90:289-304,336-351: the four indices of the 2-IP/2-EA
+// matrices).  irr = itsym of the first active orbital onward (1-based).
+__global__ void k_sym_screen(double *x, double *y, int M, int n, int k, const ll *irr) {
+    ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+    ll total = M;
+    for (int i = 0; i < k; ++i) total *= n;
+    if (t >= total) return;
+    ll r = t / M;
+    int g = 0;
+    for (int i = 0; i < k; ++i) {
+        g ^= (int)irr[r % n] - 1;
+        r /= n;
+    }
+    if (g != 0) {
+        x[t] = 0.0;
+        if (y) y[t] = 0.0;
+    }
+}
+
+void launch_sym_screen(double *x, double *y, int M, int n, int k, const long long *irr, cudaStream_t st) {
+    ll total = M;
+    for (int i = 0; i < k; ++i) total *= n;
+    k_sym_screen<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(x, y, M, n, k, irr);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+
 int launch_ijkl_tables(int nsym, const ll *nish, const ll *nash, const ll *nssh, int norb, ll *its, ll *itsym,
                        ll *num, ll *indic, ll *jndic, ll *ndeb, ll *nad, ll *kt, ll *ni4, int *bad, cudaStream_t st) {
     k_ijkl_tables<<<1, 256, 0, st>>>(nsym, nish, nash, nssh, norb, its, itsym, num, indic, jndic, ndeb, nad, kt, ni4,

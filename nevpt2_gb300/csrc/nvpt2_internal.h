@@ -56,6 +56,7 @@ int launch_ijkl_tables(int nsym, const long long *nish, const long long *nash, c
                        long long *its, long long *itsym, long long *num, long long *indic, long long *jndic,
                        long long *ndeb, long long *nad, long long *kt, long long *ni4, int *bad, cudaStream_t st);
 void launch_ai_twoint(const IjklTables &T, long long count, const int64_t *ijkl, double *out, cudaStream_t st);
+void launch_sym_screen(double *x, double *y, int M, int n, int k, const long long *irr, cudaStream_t st);
 void launch_aj_atwo_twoint(const IjklTables &T, const double *oneint, int n, int ncore, int norb, double *atwo,
                            double *aj, cudaStream_t st);
 // Kernel spans for live measurement (nvpt_set_profiling): when enabled, a

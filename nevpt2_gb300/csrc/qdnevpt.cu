@@ -699,8 +699,11 @@ class Runner {
             if (smem > 227 * 1024) throw Error(NVPT_EINVAL, "resolvent: pencil order above the shared-memory limit");
             ck(cudaFuncSetAttribute(k_tridiag_resolvent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                "smem attr");
+            ProfSpan sp;
+            sp.begin("pencil_solve", c.st, 0);
             k_tridiag_resolvent<<<(unsigned)L, 128, smem, c.st>>>(PT.d.p, PT.e.p, n, Yt.p, Yt.sh[1], L, M - 1, sg.p,
                                                                    a.p);
+            sp.end();
             LAUNCHED();
         }
         return download(c, a.p, 2 + 8);

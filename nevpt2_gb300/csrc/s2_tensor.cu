@@ -470,11 +470,18 @@ bool pencil_tridiag(Ctx &c, const double *K, const double *S, long long n, Penci
     int lw_p = 0;
     ck(cusolverDnDpotrf_bufferSize(c.sol, CUBLAS_FILL_MODE_UPPER, N, P.U.p, N, &lw_p), "potrf_bufferSize");
     SolverWork sw(c, lw_p);
+    ProfSpan sp;
+    sp.begin("pencil_potrf", c.st, 0);
     ck(cusolverDnDpotrf(c.sol, CUBLAS_FILL_MODE_UPPER, N, P.U.p, N, sw.w, lw_p, sw.info), "potrf");
+    sp.end();
     if (sw.status() != 0) return false;
+    sp.begin("pencil_reduce", c.st, 0);
     reduce_to_standard(c, P.A.p, P.U.p, n);
-    if (sytrd_lower(c, P.A.p, n, P.d.p, P.e.p, P.tau.p, true, std::min(4, std::max(1, c.sm_share))) != 0)
-        throw Error(4, "tridiagonalisation: a grid barrier timed out");
+    sp.end();
+    sp.begin("pencil_sytrd", c.st, 0);
+    const int trc = sytrd_lower(c, P.A.p, n, P.d.p, P.e.p, P.tau.p, true, std::min(4, std::max(1, c.sm_share)));
+    sp.end();
+    if (trc != 0) throw Error(4, "tridiagonalisation: a grid barrier timed out");
     return true;
 }
 
@@ -482,6 +489,8 @@ void pencil_rhs(Ctx &c, const PencilTridiag &P, double *Y, long long m) {
     if (P.n == 0 || m == 0) return;
     const int N = (int)P.n, Mc = (int)m;
     const double one = 1.0;
+    ProfSpan sp;
+    sp.begin("pencil_rhs", c.st, 0);
     ck(cublasDtrsm(c.blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, N, Mc, &one,
                    P.U.p, N, Y, N),
        "trsm");
@@ -493,6 +502,7 @@ void pencil_rhs(Ctx &c, const PencilTridiag &P, double *Y, long long m) {
     ck(cusolverDnDormtr(c.sol, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, N, Mc, P.A.p, N, P.tau.p, Y, N,
                         sw.w, lw, sw.info),
        "ormtr");
+    sp.end();
     const int st = sw.status();
     if (st != 0) throw Error(2, "ormtr failed, info=" + std::to_string(st));
 }

@@ -103,21 +103,26 @@ def get_aj_atwo(nact: int, ncore: int, norb: int, oneint, cholesky_array):
     return atwo, aj
 
 
-def koop_matrices_ctl(metat: int, nact: int, ncore: int, atwo, daaa, taa, dal, f, aj) -> dict:
-    """src/koop_matrices.F90:16 koop_matrices_ctl.  ``f`` is updated in place."""
+def koop_matrices_ctl(metat: int, nact: int, ncore: int, atwo, daaa, taa, dal, f, aj, ctx: Context | None = None) -> dict:
+    """src/koop_matrices.F90:16 koop_matrices_ctl.  ``f`` is updated in place.
+    On a context with symmetry tables (SymmetryIntegrals) koop2E's irrep
+    screen applies."""
     n, M = nact, metat
     out = {"1-IPKO": _z(M, n, n), "1-EAKO": _z(M, n, n), "2-HRDM": _z(M, n, n, n, n), "2-IPKO": _z(M, n, n, n, n),
            "2-EAKO": _z(M, n, n, n, n), "gk0pa": _z(M, n, n, n, n), "gk0pd": _z(M, n, n, n, n), "gk0pf": _z(M, n, n)}
-    context().call("nvpt_koop_matrices_ctl", M, n, ncore, ptr(_f(atwo)), ptr(_f(daaa)), ptr(_f(taa)), ptr(_f(dal)),
+    (ctx or context()).call("nvpt_koop_matrices_ctl", M, n, ncore, ptr(_f(atwo)), ptr(_f(daaa)), ptr(_f(taa)), ptr(_f(dal)),
                    ptr(f), ptr(_f(aj)), *[ptr(out[k]) for k in ("1-IPKO", "1-EAKO", "2-HRDM", "2-IPKO", "2-EAKO",
                                                                "gk0pa", "gk0pd", "gk0pf")])
     return out
 
 
-def bamat(atwo, ro4, daaa, taa, dal, nact: int, ncore: int, f, aj, norb: int, metat: int, nsym: int = 1):
-    """src/koopro4QD.F90:3974 bamat -> (amat "amatIP", atmat "amatEA")."""
+def bamat(atwo, ro4, daaa, taa, dal, nact: int, ncore: int, f, aj, norb: int, metat: int, nsym: int = 1,
+          ctx: Context | None = None):
+    """src/koopro4QD.F90:3974 bamat -> (amat "amatIP", atmat "amatEA").
+    nsym > 1 (the symmetry-screened branch) needs a context with the
+    matching symmetry tables (SymmetryIntegrals.ctx)."""
     amat, atmat = _z(metat, *(nact,) * 6), _z(metat, *(nact,) * 6)
-    context().call("nvpt_bamat", ptr(amat), ptr(atmat), ptr(_f(atwo)), ptr(_f(ro4)), ptr(_f(daaa)), ptr(_f(taa)),
+    (ctx or context()).call("nvpt_bamat", ptr(amat), ptr(atmat), ptr(_f(atwo)), ptr(_f(ro4)), ptr(_f(daaa)), ptr(_f(taa)),
                    ptr(_f(dal)), nact, ncore, ptr(f), ptr(_f(aj)), norb, metat, nsym)
     return amat, atmat
 
@@ -153,7 +158,10 @@ class SymmetryIntegrals:
     KEYS = ("its", "itsym", "num", "indic", "jndic", "ndeb", "nad", "kt")
 
     def __init__(self, nish, nash, nssh, ctx: Context | None = None):
-        self.ctx = ctx or context()
+        # a context of its own unless one is given: the tables are that
+        # context's integral state and switch on the symmetry screens of
+        # koop_matrices_ctl and bamat on it
+        self.ctx = ctx or Context(0)
         self.nsym = len(nish)
         c = [np.ascontiguousarray(x, dtype=np.int64) for x in (nish, nash, nssh)]
         ni4 = np.zeros(1, np.int64)

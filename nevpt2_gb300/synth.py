@@ -288,3 +288,76 @@ def batch_problems(count: int = 64, seed: int = BATCH_SEED, first: int = 0):
         out.append(make_problem(n, n, nc, nv, metat=3, ndet=None if full <= 20_000 else 20_000, seed=seed + pid,
                                 with_trdm=True))
     return out
+
+
+def orbital_irreps(nish, nash, nssh) -> np.ndarray:
+    """itsym of src/infsym.F90:38-69: irrep (1-based) of every orbital,
+    inactive irrep by irrep, then active, then secondary."""
+    out = []
+    for cnt in (nish, nash, nssh):
+        for r, k in enumerate(cnt):
+            out += [r + 1] * int(k)
+    return np.array(out, dtype=np.int64)
+
+
+def symmetric_chol(itsym, nchovec: int, rng: np.random.Generator) -> np.ndarray:
+    """DF vectors that respect point-group symmetry: vector Q carries one
+    irrep and L[Q, pq] vanishes unless irrep(p) x irrep(q) is that irrep, so
+    (pq|rs) vanishes unless irrep(pq) = irrep(rs)."""
+    itsym = np.asarray(itsym)
+    norb = itsym.size
+    gq = rng.integers(0, int(itsym.max()), nchovec)
+    L = np.zeros((nchovec, npair(norb)), order="F")
+    col = 0
+    for p in range(norb):
+        for q in range(p + 1):
+            sd = 0.05 * np.exp(-abs(p - q) / 8.0)
+            L[:, col] = np.where(gq == ((itsym[p] - 1) ^ (itsym[q] - 1)), rng.standard_normal(nchovec) * sd, 0.0)
+            col += 1
+    return L
+
+
+def make_sym_problem(nish, nash, nssh, nele: int, metat: int = 1, ndet: int | None = None, seed: int = 7,
+                     irrep: int = 1) -> Problem:
+    """A problem with point-group symmetry: determinants of one total irrep
+    (product of the irreps of every occupied active spin orbital), so the
+    RDMs vanish exactly where symmetry forbids them; symmetric DF integrals
+    and a one-electron operator coupling only orbitals of equal irrep.
+    Problem.chol holds the DF vectors (the twoint list is built from them)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    itsym = orbital_irreps(nish, nash, nssh)
+    ncore, nact = int(sum(nish)), int(sum(nash))
+    nvirt = itsym.size - ncore - nact
+    asym = itsym[ncore:ncore + nact] - 1
+    na, nb = nele - nele // 2, nele // 2
+
+    def irr(mask):
+        g = 0
+        for k in range(nact):
+            if mask >> k & 1:
+                g ^= int(asym[k])
+        return g
+
+    sa, sb = strings(nact, na), strings(nact, nb)
+    ga = np.array([irr(int(m)) for m in sa]), np.array([irr(int(m)) for m in sb])
+    pairs = [(i, j) for i in range(sa.size) for j in range(sb.size) if (ga[0][i] ^ ga[1][j]) == irrep - 1]
+    if ndet is not None and ndet < len(pairs):
+        pick = np.sort(rng.choice(len(pairs), size=ndet, replace=False))
+        pairs = [pairs[k] for k in pick]
+    amask = np.array([sa[i] for i, _ in pairs], dtype=np.uint32)
+    bmask = np.array([sb[j] for _, j in pairs], dtype=np.uint32)
+    C = rng.standard_normal((amask.size, metat))
+    Qm, R = np.linalg.qr(C)
+    coef = np.asfortranarray(Qm[:, :metat] * np.sign(np.diag(R)[:metat])[None, :])
+    dal, taa, daaa, ro4 = rdms(nact, amask, bmask, coef, True)
+    norb = itsym.size
+    chol = symmetric_chol(itsym, 4 * norb, rng)
+    eps = np.concatenate([np.sort(rng.uniform(-2.0, -0.5, ncore)), np.sort(rng.uniform(-0.5, 0.5, nact)),
+                          np.sort(rng.uniform(0.5, 5.0, nvirt))])
+    off = rng.normal(0.0, 1e-3, (norb, norb)) * (itsym[:, None] == itsym[None, :])
+    F = np.diag(eps) + np.triu(off, 1) + np.triu(off, 1).T
+    h1 = F - fock_two_electron(chol, norb, ncore, nact, dal[0])
+    oneint = np.array([h1[p, q] for p in range(norb) for q in range(p + 1)])
+    return Problem(nact=nact, nele=nele, ncore=ncore, nvirt=nvirt, metat=metat, nchovec=chol.shape[0], seed=seed,
+                   amask=amask, bmask=bmask, coef=coef, dal=dal, taa=taa, daaa=daaa, ro4=ro4, oneint=oneint,
+                   chol=chol, eps=eps, energies=np.zeros(metat))

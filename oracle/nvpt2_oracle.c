@@ -51,7 +51,10 @@ typedef struct {
     I n, M, W;
     I *lindi, *lindj, *lindk, *normind; /* normind(n,n,n,n) column-major */
     const double *d1, *d2, *d3, *ro4;   /* dal, taa, daaa, ro4            */
+    const I *asym;                      /* irrep (1-based) of each active orbital, NULL = C1 */
 } orc_ctx;
+/* its(i,j) of infsym.F90:34 (D2h product table) */
+static inline I o_its(I i, I j) { return ((i - 1) ^ (j - 1)) + 1; }
 
 #define D1(c, s, a, b) ((c)->d1[((s)-1) + (c)->M * (((a)-1) + (c)->n * ((b)-1))])
 #define D2(c, s, a, b, cc, d)                                                  \
@@ -87,6 +90,7 @@ static I o_norm(I a, I b, I c, I d) {
 static void o_init(orc_ctx *c, I n, I M) {
     c->n = n;
     c->M = M;
+    c->asym = NULL;
     c->lindi = (I *)malloc(sizeof(I) * n);
     c->lindj = (I *)malloc(sizeof(I) * n);
     c->lindk = (I *)malloc(sizeof(I) * n);
@@ -495,6 +499,10 @@ static void o_koop2E(const orc_ctx *c, const double *atwo, double *koopaa, doubl
             for (I ap = 1; ap <= n; ++ap)
                 for (I bp = 1; bp <= n; ++bp) {
                     for (I s = 1; s <= M; ++s) OUT5(koopaa, s, ap, bp, a, b) = 0.0;
+                    /* koop_matrices.F90:289-304: skip when its(isab, iscd) /= 1 */
+                    if (c->asym && o_its(o_its(c->asym[a - 1], c->asym[b - 1]),
+                                         o_its(c->asym[bp - 1], c->asym[ap - 1])) != 1)
+                        continue;
                     for (I d = 1; d <= n; ++d) {
                         I jad = FIDX(a + ncore, d + ncore), jbd = FIDX(b + ncore, d + ncore);
                         for (I s = 1; s <= M; ++s)
@@ -523,6 +531,10 @@ static void o_koop2E(const orc_ctx *c, const double *atwo, double *koopaa, doubl
             for (I ap = 1; ap <= n; ++ap)
                 for (I bp = 1; bp <= n; ++bp) {
                     for (I s = 1; s <= M; ++s) OUT5(koopeaa, s, ap, bp, a, b) = 0.0;
+                    /* koop_matrices.F90:336-351: the same screen */
+                    if (c->asym && o_its(o_its(c->asym[a - 1], c->asym[b - 1]),
+                                         o_its(c->asym[bp - 1], c->asym[ap - 1])) != 1)
+                        continue;
                     for (I cc = 1; cc <= n; ++cc) {
                         I jac = FIDX(a + ncore, cc + ncore), jbc = FIDX(b + ncore, cc + ncore);
                         for (I s = 1; s <= M; ++s) {
@@ -643,13 +655,13 @@ static void o_koopman0pE(const orc_ctx *c, const double *atwo, double *koopaa, d
  *   ipko2 (M,n^4) "2-IPKO" (the 2-HRDM buffer is overwritten by koop2E in the
  *   reference, so "2-HRDM" is snapshotted before); eako2 "2-EAKO";
  *   gk0pa, gk0pd (M,n^4); gk0pf (M,n,n).  f is the in/out scratch. */
-void orc_koop_matrices_ctl(I metat, I nact, I ncore, const double *atwo, const double *daaa, const double *taa,
-                           const double *dal, double *f, const double *aj, double *ipko1, double *eako1,
-                           double *hrdm2, double *ipko2, double *eako2, double *gk0pa, double *gk0pd,
-                           double *gk0pf) {
+void orc_koop_matrices_ctl_sym(I metat, I nact, I ncore, const double *atwo, const double *daaa, const double *taa,
+                               const double *dal, double *f, const double *aj, double *ipko1, double *eako1,
+                               double *hrdm2, double *ipko2, double *eako2, double *gk0pa, double *gk0pd,
+                               double *gk0pf, const I *asym) {
     orc_ctx c;
     memset(&c, 0, sizeof c);
-    c.n = nact; c.M = metat; c.d1 = dal; c.d2 = taa; c.d3 = daaa;
+    c.n = nact; c.M = metat; c.d1 = dal; c.d2 = taa; c.d3 = daaa; c.asym = asym;
     I n = nact, M = metat;
     o_koopE(&c, atwo, ipko1, eako1, ncore, f, aj);
     for (I i = 1; i <= n; ++i)
@@ -662,6 +674,14 @@ void orc_koop_matrices_ctl(I metat, I nact, I ncore, const double *atwo, const d
     o_koop2E(&c, atwo, ipko2, eako2, ncore, f, aj);
     /* koopman0pE reuses the koopaa buffer: it fully overwrites it (gk0pa). */
     o_koopman0pE(&c, atwo, gk0pa, gk0pd, gk0pf, ncore, f, aj);
+}
+
+void orc_koop_matrices_ctl(I metat, I nact, I ncore, const double *atwo, const double *daaa, const double *taa,
+                           const double *dal, double *f, const double *aj, double *ipko1, double *eako1,
+                           double *hrdm2, double *ipko2, double *eako2, double *gk0pa, double *gk0pd,
+                           double *gk0pf) {
+    orc_koop_matrices_ctl_sym(metat, nact, ncore, atwo, daaa, taa, dal, f, aj, ipko1, eako1, hrdm2, ipko2, eako2,
+                              gk0pa, gk0pd, gk0pf, NULL);
 }
 
 /* koop_matrices.F90:591-619 fdiff_F: per state max |F|. */
@@ -689,9 +709,17 @@ void orc_fdiff_F(const double *koopab, I nact, I metat, double *maxabs) {
 static void o_bamat_unit(const orc_ctx *cx, double *amat, double *atmat, const double *atwo, const double *f,
                          I n, I ncore, I M, I slab, I ap) {
     const I a = slab / n + 1, cc = slab % n + 1;
+    const I *sy = cx->asym; /* koopro4QD.F90:4105-4228 when set */
             for (I b = 1; b <= n; ++b) {
                     for (I bp = 1; bp <= n; ++bp)
-                        for (I cp = 1; cp <= n; ++cp)
+                        for (I cp = 1; cp <= n; ++cp) {
+                            I isabcp = 1, isa = 1, isb = 1, isc = 1;
+                            if (sy) {
+                                isa = sy[a - 1]; isb = sy[b - 1]; isc = sy[cc - 1];
+                                const I isabc = o_its(o_its(isa, isb), isc);
+                                isabcp = o_its(o_its(sy[ap - 1], sy[bp - 1]), sy[cp - 1]);
+                                if (o_its(isabc, isabcp) != 1) continue;
+                            }
                             for (I d = 1; d <= n; ++d) {
                                 double fda = f[FIDX(d + ncore, a + ncore)];
                                 double fcd = f[FIDX(cc + ncore, d + ncore)];
@@ -723,37 +751,53 @@ static void o_bamat_unit(const orc_ctx *cx, double *amat, double *atmat, const d
                                         OUT7(amat, s, ap, bp, cp, a, b, cc) += dum1 * dint1 - 0.5 * (dum2 * dint2 + dum3 * dint3 - dum4 * dint4);
                                         OUT7(atmat, s, ap, bp, cp, a, b, cc) += 0.5 * dum4t * dint4;
                                     }
-                                    for (I ief = 1; ief <= n; ++ief)
-                                        for (I s = 1; s <= M; ++s) {
-                                            double di1 = ATWO(d, ief, ie, a);
-                                            double e1 = o_eeee(cx, cp, ap, bp, b, d, ief, ie, cc, s);
-                                            double e1t = -e1;
-                                            if (bp == b) e1t += 2.0 * o_eee2(cx, cp, ap, d, ief, ie, cc, s);
-                                            OUT7(amat, s, ap, bp, cp, a, b, cc) += e1 * di1;
-                                            OUT7(atmat, s, ap, b, cp, a, bp, cc) += e1t * di1;
-                                            double e2 = o_eeee(cx, cp, ap, bp, b, d, ief, a, ie, s);
-                                            double e2t = -e2;
-                                            if (bp == b) e2t += 2.0 * o_eee2(cx, cp, ap, d, ief, a, ie, s);
-                                            double di2 = ATWO(d, ief, cc, ie);
-                                            OUT7(amat, s, ap, bp, cp, a, b, cc) -= e2 * di2;
-                                            OUT7(atmat, s, ap, b, cp, a, bp, cc) -= e2t * di2;
-                                            double e3 = o_eeee(cx, cp, ap, bp, ie, d, ief, a, cc, s);
-                                            double e3t = o_eeeet(cx, cp, ap, bp, ie, d, ief, a, cc, s);
-                                            double di3 = ATWO(d, ief, b, ie);
-                                            OUT7(amat, s, ap, bp, cp, a, b, cc) -= e3 * di3;
-                                            OUT7(atmat, s, ap, bp, cp, a, b, cc) += e3t * di3;
+                                    for (I ief = 1; ief <= n; ++ief) {
+                                        int t1 = 1, t2 = 1, t3 = 1;
+                                        if (sy) {
+                                            const I isfde = o_its(o_its(sy[ief - 1], sy[d - 1]), sy[ie - 1]);
+                                            const I istot = o_its(isabcp, isfde);
+                                            t1 = o_its(isfde, isa) == 1 && o_its(istot, o_its(isb, isc)) == 1;
+                                            t2 = o_its(isfde, isc) == 1 && o_its(istot, o_its(isa, isb)) == 1;
+                                            t3 = o_its(isfde, isb) == 1 && o_its(istot, o_its(isa, isc)) == 1;
                                         }
+                                        for (I s = 1; s <= M; ++s) {
+                                            if (t1) {
+                                                double di1 = ATWO(d, ief, ie, a);
+                                                double e1 = o_eeee(cx, cp, ap, bp, b, d, ief, ie, cc, s);
+                                                double e1t = -e1;
+                                                if (bp == b) e1t += 2.0 * o_eee2(cx, cp, ap, d, ief, ie, cc, s);
+                                                OUT7(amat, s, ap, bp, cp, a, b, cc) += e1 * di1;
+                                                OUT7(atmat, s, ap, b, cp, a, bp, cc) += e1t * di1;
+                                            }
+                                            if (t2) {
+                                                double e2 = o_eeee(cx, cp, ap, bp, b, d, ief, a, ie, s);
+                                                double e2t = -e2;
+                                                if (bp == b) e2t += 2.0 * o_eee2(cx, cp, ap, d, ief, a, ie, s);
+                                                double di2 = ATWO(d, ief, cc, ie);
+                                                OUT7(amat, s, ap, bp, cp, a, b, cc) -= e2 * di2;
+                                                OUT7(atmat, s, ap, b, cp, a, bp, cc) -= e2t * di2;
+                                            }
+                                            if (t3) {
+                                                double e3 = o_eeee(cx, cp, ap, bp, ie, d, ief, a, cc, s);
+                                                double e3t = o_eeeet(cx, cp, ap, bp, ie, d, ief, a, cc, s);
+                                                double di3 = ATWO(d, ief, b, ie);
+                                                OUT7(amat, s, ap, bp, cp, a, b, cc) -= e3 * di3;
+                                                OUT7(atmat, s, ap, bp, cp, a, b, cc) += e3t * di3;
+                                            }
+                                        }
+                                    }
                                 }
                             }
+                        }
             }
 }
 
 static void o_bamat_range(double *amat, double *atmat, const double *atwo, const double *ro4, const double *daaa,
                           const double *taa, const double *dal, I nact, I ncore, double *f, const double *aj,
-                          I metat, I slab_lo, I slab_hi) {
+                          I metat, I slab_lo, I slab_hi, const I *asym) {
     orc_ctx c;
     o_init(&c, nact, metat);
-    c.d1 = dal; c.d2 = taa; c.d3 = daaa; c.ro4 = ro4;
+    c.d1 = dal; c.d2 = taa; c.d3 = daaa; c.ro4 = ro4; c.asym = asym;
     I n = nact, M = metat;
     o_build_f(f, aj, atwo, n, ncore, 1);
     const I units = (slab_hi - slab_lo) * n;
@@ -767,7 +811,15 @@ void orc_bamat(double *amat, double *atmat, const double *atwo, const double *ro
                const double *taa, const double *dal, I nact, I ncore, double *f, const double *aj, I norb,
                I metat) {
     (void)norb;
-    o_bamat_range(amat, atmat, atwo, ro4, daaa, taa, dal, nact, ncore, f, aj, metat, 0, nact * nact);
+    o_bamat_range(amat, atmat, atwo, ro4, daaa, taa, dal, nact, ncore, f, aj, metat, 0, nact * nact, NULL);
+}
+
+/* The symmetry-screened branch (koopro4QD.F90:4105-4228): asym = irrep of
+ * every active orbital (itsym(ncore+1..ncore+nact)). */
+void orc_bamat_sym(double *amat, double *atmat, const double *atwo, const double *ro4, const double *daaa,
+                   const double *taa, const double *dal, I nact, I ncore, double *f, const double *aj, I metat,
+                   const I *asym) {
+    o_bamat_range(amat, atmat, atwo, ro4, daaa, taa, dal, nact, ncore, f, aj, metat, 0, nact * nact, asym);
 }
 
 /* Time-bounded variant for the CPU baseline: runs the bamat iterations of the
@@ -777,7 +829,7 @@ void orc_bamat_slabs(double *amat, double *atmat, const double *atwo, const doub
                      const double *taa, const double *dal, I nact, I ncore, double *f, const double *aj, I metat,
                      I nslab) {
     if (nslab > nact * nact) nslab = nact * nact;
-    o_bamat_range(amat, atmat, atwo, ro4, daaa, taa, dal, nact, ncore, f, aj, metat, 0, nslab);
+    o_bamat_range(amat, atmat, atwo, ro4, daaa, taa, dal, nact, ncore, f, aj, metat, 0, nslab, NULL);
 }
 
 /* bamat restricted to a list of (a,c) slabs (0-based slab = (a-1) n + (c-1)):

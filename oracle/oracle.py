@@ -45,6 +45,8 @@ def lib():
         L.orc_fdiff_F.argtypes = [P, I64, I64, P]
         L.orc_bamat.argtypes = [P] * 7 + [I64, I64, P, P, I64, I64]
         L.orc_bamat_slabs.argtypes = [P] * 7 + [I64, I64, P, P, I64, I64]
+        L.orc_koop_matrices_ctl_sym.argtypes = [I64, I64, I64] + [P] * 15
+        L.orc_bamat_sym.argtypes = [P] * 7 + [I64, I64, P, P, I64, P]
         L.orc_bamat_slab_list.argtypes = [P] * 7 + [I64, I64, P, P, I64, P, I64]
         L.orc_bbmat.argtypes = [P] * 6 + [I64, I64, P, P, I64]
         L.orc_bcmat.argtypes = [P] * 6 + [I64, I64, P, P, I64]
@@ -126,6 +128,29 @@ def koop_matrices_ctl(metat, nact, ncore, atwo, daaa, taa, dal, f, aj):
                                 *[_p(out[k]) for k in ("ipko1", "eako1", "hrdm2", "ipko2", "eako2", "gk0pa",
                                                        "gk0pd", "gk0pf")])
     return out
+
+
+def koop_matrices_ctl_sym(metat, nact, ncore, atwo, daaa, taa, dal, f, aj, asym):
+    """koop_matrices_ctl with the its() screen of koop2E (koop_matrices.F90:289-351);
+    asym = irreps (1-based) of the active orbitals."""
+    n, M = nact, metat
+    out = dict(ipko1=zeros(M, n, n), eako1=zeros(M, n, n), hrdm2=zeros(M, n, n, n, n), ipko2=zeros(M, n, n, n, n),
+               eako2=zeros(M, n, n, n, n), gk0pa=zeros(M, n, n, n, n), gk0pd=zeros(M, n, n, n, n),
+               gk0pf=zeros(M, n, n))
+    sy = np.ascontiguousarray(asym, dtype=np.int64)
+    lib().orc_koop_matrices_ctl_sym(M, n, ncore, _p(atwo), _p(daaa), _p(taa), _p(dal), _p(f), _p(aj),
+                                    *[_p(out[k]) for k in ("ipko1", "eako1", "hrdm2", "ipko2", "eako2", "gk0pa",
+                                                           "gk0pd", "gk0pf")], _p(sy))
+    return out
+
+
+def bamat_sym(atwo, ro4, daaa, taa, dal, nact, ncore, f, aj, metat, asym):
+    """The symmetry-screened bamat branch (koopro4QD.F90:4105-4228)."""
+    amat, atmat = zeros(metat, *(nact,) * 6), zeros(metat, *(nact,) * 6)
+    sy = np.ascontiguousarray(asym, dtype=np.int64)
+    lib().orc_bamat_sym(_p(amat), _p(atmat), _p(atwo), _p(ro4), _p(daaa), _p(taa), _p(dal), nact, ncore, _p(f),
+                        _p(aj), metat, _p(sy))
+    return amat, atmat
 
 
 def fdiff_F(gk0pf, nact, metat):

@@ -124,3 +124,69 @@ def test_init_rejects_bad_counts(gpu_ctx):
     si = koopro.SymmetryIntegrals([1, 1], [1, 1], [1, 1])
     with pytest.raises(_native.NvptError):
         si.ai(np.array([[1, 1, 1, 7]]))  # twoint not set yet
+
+
+# ------------------------------------------- symmetry-screened Koopmans builders
+SYM = [([1, 1], [2, 2], [2, 2], 4, 1), ([1, 0, 1, 0], [2, 1, 2, 1], [1, 1, 1, 1], 6, 2)]
+
+
+def _sym_inputs(case):
+    from nevpt2_gb300 import synth
+    nish, nash, nssh, ne, M = case
+    p = synth.make_sym_problem(nish, nash, nssh, ne, metat=M, seed=5)
+    t = orc.ijkl_tables(nish, nash, nssh)
+    tw = orc.pack_twoint(t, p.chol)
+    asym = t["itsym"][p.ncore:p.ncore + p.nact]
+    return p, t, tw, asym
+
+
+@pytest.mark.parametrize("case", range(len(SYM)))
+def test_oracle_screened_branches_equal_c1_on_symmetric_inputs(case):
+    """The terms the reference's symmetry branches skip vanish on symmetric
+    inputs: the screened and the C1 loops agree (CPU, oracle)."""
+    p, t, tw, asym = _sym_inputs(SYM[case])
+    n, nc, M = p.nact, p.ncore, p.metat
+    atwo, aj = orc.get_aj_atwo_twoint(t, tw, p.oneint, n, nc, p.norb)
+    f1, f2 = np.zeros_like(aj), np.zeros_like(aj)
+    a = orc.koop_matrices_ctl(M, n, nc, atwo, p.daaa, p.taa, p.dal, f1, aj)
+    b = orc.koop_matrices_ctl_sym(M, n, nc, atwo, p.daaa, p.taa, p.dal, f2, aj, asym)
+    for k in ("ipko2", "eako2"):
+        assert np.abs(a[k] - b[k]).max() <= 1e-12 * max(np.abs(a[k]).max(), 1.0)
+    A, At = orc.bamat(atwo, p.ro4, p.daaa, p.taa, p.dal, n, nc, f1, aj, p.norb, M)
+    B, Bt = orc.bamat_sym(atwo, p.ro4, p.daaa, p.taa, p.dal, n, nc, f2, aj, M, asym)
+    assert np.abs(A - B).max() <= 1e-12 * np.abs(A).max()
+    assert np.abs(At - Bt).max() <= 1e-12 * np.abs(At).max()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", range(len(SYM)))
+def test_symmetry_screened_builders_against_oracle(gpu_ctx, case):
+    from conftest import rel_err
+    from nevpt2_gb300 import _native, koopro
+    p, t, tw, asym = _sym_inputs(SYM[case])
+    nish, nash, nssh = SYM[case][:3]
+    n, nc, M = p.nact, p.ncore, p.metat
+    si = koopro.SymmetryIntegrals(nish, nash, nssh)
+    si.set_twoint(tw)
+    atwo, aj = si.get_aj_atwo(n, nc, p.oneint)
+    ratwo, raj = orc.get_aj_atwo_twoint(t, tw, p.oneint, n, nc, p.norb)
+    f, rf = np.zeros_like(aj), np.zeros_like(aj)
+    got = koopro.koop_matrices_ctl(M, n, nc, atwo, p.daaa, p.taa, p.dal, f, aj, ctx=si.ctx)
+    ref = orc.koop_matrices_ctl_sym(M, n, nc, ratwo, p.daaa, p.taa, p.dal, rf, raj, asym)
+    for k, rk in (("2-IPKO", "ipko2"), ("2-EAKO", "eako2"), ("1-IPKO", "ipko1"), ("gk0pa", "gk0pa")):
+        assert rel_err(got[k], ref[rk]) < 1e-10, k
+    A, At = koopro.bamat(atwo, p.ro4, p.daaa, p.taa, p.dal, n, nc, f, aj, p.norb, M, nsym=len(nish), ctx=si.ctx)
+    R, Rt = orc.bamat_sym(ratwo, p.ro4, p.daaa, p.taa, p.dal, n, nc, rf, raj, M, asym)
+    assert rel_err(A, R) < 1e-10 and rel_err(At, Rt) < 1e-10
+    # elements the reference never assigns are exactly zero
+    irr = asym - 1
+    tot = np.zeros((n,) * 6, dtype=np.int64)
+    for ax in range(6):
+        sh = [1] * 6
+        sh[ax] = n
+        tot = tot ^ irr.reshape(sh)
+    assert np.all(A[:, tot != 0] == 0.0) and np.all(At[:, tot != 0] == 0.0)
+    # without the tables the symmetry branch is refused
+    with pytest.raises(_native.NvptError) as e:
+        koopro.bamat(atwo, p.ro4, p.daaa, p.taa, p.dal, n, nc, f, aj, p.norb, M, nsym=len(nish))
+    assert e.value.status == 4
