@@ -499,6 +499,24 @@ def run_ours(args):
 
     fp64_floor = ulp_sensitivity()
 
+    # the partial trace Gamma4 -> Gamma3 (bro3) alone: HBM roofline on the
+    # distinct packed entries it reads plus the n^6 outputs it writes
+    def bro3_alone():
+        ctx.call("nvpt_set_profiling", 1)
+        res = []
+        for _ in range(3):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                ctx.call("nvpt_bro3_d", ptr(st.ro4), ptr(st.daaa), n, p.nele, M, ptr_stream(stream))
+            torch.cuda.synchronize(dev)
+            t_ms, t_n, t_b = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
+            ctx.call("nvpt_profile_read", b"bro3", ctypes.byref(t_ms), ctypes.byref(t_n), ctypes.byref(t_b))
+            res.append(t_ms.value)
+        ctx.call("nvpt_set_profiling", 0)
+        return float(np.median(res))
+
+    bro3_ms = bro3_alone()
+
     # device time of the stage-2 pieces in one FP64 step (spans on the pieces'
     # own streams; they overlap in time, so they do not add up to the step)
     S2_TAGS = ["s2_prepare", "s2_class_0", "s2_class_+1", "s2_class_-1", "s2_class_+2", "s2_class_-2",
@@ -599,8 +617,12 @@ def run_ours(args):
     # DGEMMs); algorithmic flops of the reference loop 12n^9 + 16n^8 + 12n^7
     # per state, against the FP64 DGEMM rate measured in this run.
     alg_flops = M * (12 * n**9 + 16 * n**8 + 12 * n**7)
+    # what the dense reformulation executes: four n^3-deep products per slab
+    # (8 n^9) and the n^8 lower-order GEMMs (4 n^8)
+    exec_flops = M * (8 * n**9 + 4 * n**8)
     peak64 = fp64_peak(dev)
     achieved = alg_flops / (bamat_ms * 1e-3) / 1e12
+    achieved_exec = exec_flops / (bamat_ms * 1e-3) / 1e12
     # roofline (split path): the Ozaki product kernel streams digit tiles
     # (9 BF16 digits per FP64 element) from HBM once; algorithmic bytes per
     # launch = all digits of X and A + the FP64 results.
@@ -617,6 +639,10 @@ def run_ours(args):
     # products per FP64-equivalent product; tensor-bound
     bf16_peak = pk.get("bf16_tflops", 1900.0)
     ow_tf = 64 * ow_fl.value / (ow_ms.value * 1e-3) / 1e12 if ow_ms.value > 0 else None
+    from oracle import oracle as orc
+    touched = orc.bro3_touched(n)
+    bro3_bytes = 8 * M * (touched + n**6)
+    bro3_gbs = bro3_bytes / (bro3_ms * 1e-3) / 1e9
     de = lambda a_, b_: float(np.abs(np.asarray(a_) - np.asarray(b_)).max())
     koop = {k: st.result(k) for k in st.out}
     koop.update({"1-RDM": p.dal, "2-RDM": p.taa, "3-RDM": p.daaa})
@@ -627,8 +653,11 @@ def run_ours(args):
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded CI vector, exact RDMs, random DF integrals)",
             "config": workload_desc(p), "gpu_launches": int(launches),
             "e2e": {"value": e2e, "unit": "s/state", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-            "roofline": {"kernel": "bamat (k_bamat_slabs_t + cuBLAS DGEMM + k_rest_*)", "bound": "tensor",
+            "roofline": {"kernel": "bamat (k_bamat_slabs_t + k_dgemm_skinny + k_rest_*)", "bound": "fp64 pipe",
                          "achieved": achieved, "peak": peak64, "unit": "TFLOP/s", "frac": achieved / peak64,
+                         "achieved_executed": achieved_exec, "frac_executed": achieved_exec / peak64,
+                         "note": "achieved counts the reference loop's 12n^9+16n^8+12n^7 flops per state; the dense "
+                                 "reformulation executes 8n^9+4n^8 (achieved_executed, frac_executed)",
                          "traffic": None, "precision": "fp64",
                          "peak_source": "FP64 DGEMM rate measured live in this run (cuBLAS 4096^3)",
                          "kernel_ms": bamat_ms, "alg_flops": alg_flops},
@@ -657,6 +686,12 @@ def run_ours(args):
                           "fp64_equivalent_tflops": (ow_tf / 64) if ow_tf else None,
                           "kernel_ms": (ow_ms.value / ow_n.value) if ow_n.value else None},
                       "clocks": clk_sp, "step_ms_all": times_sp},
+            "roofline_bro3": {"kernel": "bro3 (k_bro3_case_a + k_bro3_combine)", "bound": "hbm", "achieved": bro3_gbs,
+                              "peak": hbm_peak, "unit": "GB/s", "frac": bro3_gbs / hbm_peak, "traffic": None,
+                              "kernel_ms": bro3_ms, "alg_bytes": bro3_bytes,
+                              "alg_bytes_def": "8 bytes x (distinct packed Gamma4 entries read, counted by the oracle's "
+                                               "ord8 enumeration, + n^6 outputs) per state",
+                              "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
             "stage2_ms_per_piece": s2_breakdown,
             "energies": energy_summary(energies),
             "clocks": clk, "cpu_baseline": cb, "step_ms_all": times}

@@ -356,7 +356,8 @@ int nvpt_bro3_d(nvpt_context *ctx, const double *ro4, double *daaa, int64_t nact
     NV_TRY(check_nact(ctx, nact, metat));
     if (nele <= 3) return fail(ctx, NVPT_EINVAL, "bro3 needs nele > 3 (it divides by nele-3)");
     Rdm r = make_rdm(nact, metat, nullptr, nullptr, nullptr, ro4);
-    launch_bro3(r, daaa, (int)nele, pick(ctx, stream));
+    if (launch_bro3(r, daaa, (int)nele, pick(ctx, stream)) != 0)
+        return fail(ctx, NVPT_ENOMEM, "bro3: device allocation failed");
     return after_launch(ctx, "bro3");
 }
 

@@ -10,6 +10,9 @@
 
 #include <cublas_v2.h>
 
+#include <algorithm>
+#include <vector>
+
 namespace nvpt {
 
 #define ATWO(i, j, k, l) atwo[((i)-1) + (ll)n * (((j)-1) + (ll)n * (((k)-1) + (ll)n * ((l)-1)))]
@@ -40,22 +43,78 @@ __global__ void k_build_f(double *f, const double *aj, const double *atwo, int n
 
 // ---------------------------------------------------------------------------
 // src/koopro4QD.F90:4881-4959 bro3.
-__global__ void k_bro3(Rdm r, double *daaa, double inv) {
+// bro3 as two passes over case-A terms.  Each term of the reference's sum,
+// ro4[ord8(i,j,k,l; ii,jj,kk,l)], is read with the key taken from the group
+// of larger normind (the first on ties).  Call a term "case A" for the output
+// O = (i,j,k; ii,jj,kk) when that is the first group.  A term of O that is
+// not case A is, entry for entry, a strict case-A term of the transposed
+// output O^T = (ii,jj,kk; i,j,k): ord8 sees the same key group with the same
+// partner.  So with
+//   P[O] = sum of the case-A terms of O,  Q[O] = the strict (>) ones,
+// daaa[O] = (P[O] + Q[O^T]) / (nele - 3).  In the first pass one CTA owns
+// the column group (ii,jj,kk) and its threads the rows (i,j,k): every term's
+// partner is a permutation of (ii,jj,kk,l), so a CTA reads at most 24 n
+// columns of ro4, each W contiguous doubles, and the CTAs of the
+// permutations of one multiset -- which read the same columns -- run side by
+// side (blockIdx orders them together).  The second pass is a tiled
+// transpose-add.  Summation order per element: the case-A terms in l order,
+// then the others in l order (the reference adds all in l order).
+constexpr int kBro3States = 8;  // states per pass of the first kernel
+__global__ void __launch_bounds__(256) k_bro3_case_a(Rdm r, const int *col_order, int s0, int ns, double *P,
+                                                     double *Q) {
     const int n = r.n, M = r.M;
-    ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
-    ll n6 = (ll)n * n * n * n * n * n;
-    if (t >= n6) return;
-    int x[6];
-    decode(t, n, 6, x);
-    const int i = x[0], j = x[1], k = x[2], ii = x[3], jj = x[4], kk = x[5];
-    for (int s = 1; s <= M; ++s) {
-        double acc = 0.0;
+    const ll n3 = (ll)n * n * n;
+    const int c = col_order[blockIdx.x];
+    const int ii = c % n + 1, jj = (c / n) % n + 1, kk = c / (n * n) + 1;
+    for (ll rr = threadIdx.x; rr < n3; rr += blockDim.x) {
+        const int i = (int)(rr % n) + 1, j = (int)((rr / n) % n) + 1, k = (int)(rr / ((ll)n * n)) + 1;
+        double p[kBro3States], q[kBro3States];
+#pragma unroll
+        for (int t = 0; t < kBro3States; ++t) p[t] = q[t] = 0.0;
         for (int l = 1; l <= n; ++l) {
+            const int n1 = normind4(i, j, k, l), n2 = normind4(ii, jj, kk, l);
+            if (n1 < n2) continue;
             int q0, q1, q2, q3;
-            int ind = ord8_key(i, j, k, l, ii, jj, kk, l, q0, q1, q2, q3);
-            acc += r.R4(ind, q0, q1, q2, q3, s);
+            const int ind = ord8_key(i, j, k, l, ii, jj, kk, l, q0, q1, q2, q3);
+#pragma unroll
+            for (int t = 0; t < kBro3States; ++t) {
+                if (t >= ns) break;
+                const double x = r.R4(ind, q0, q1, q2, q3, s0 + t + 1);
+                p[t] += x;
+                if (n1 > n2) q[t] += x;
+            }
         }
-        daaa[(s - 1) + (ll)M * t] = acc * inv;
+        const ll o = (ll)M * (rr + n3 * c);
+        for (int t = 0; t < ns; ++t) {
+            P[o + s0 + t] = p[t];
+            Q[o + s0 + t] = q[t];
+        }
+    }
+}
+
+// daaa[s, r, c] = (P[s, r, c] + Q[s, c, r]) * inv over the n^3 x n^3 matrix
+// of each state (r = (i,j,k), c = (ii,jj,kk), r fastest), 32 x 32 tiles
+// through shared memory so both reads and the write are coalesced.
+__global__ void __launch_bounds__(256) k_bro3_combine(const double *P, const double *Q, double *daaa, ll n3, int M,
+                                                      double inv) {
+    __shared__ double t[32][33];
+    const ll r0 = (ll)blockIdx.x * 32, c0 = (ll)blockIdx.y * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int s = 0; s < M; ++s) {
+        // Q tile at (row c0.., col r0..): element Q[s, c, r] with c fastest
+        for (int y = ty; y < 32; y += 8) {
+            const ll c = c0 + tx, rr = r0 + y;
+            t[y][tx] = (c < n3 && rr < n3) ? Q[s + (ll)M * (c + n3 * rr)] : 0.0;
+        }
+        __syncthreads();
+        for (int y = ty; y < 32; y += 8) {
+            const ll rr = r0 + tx, c = c0 + y;
+            if (rr < n3 && c < n3) {
+                const ll o = s + (ll)M * (rr + n3 * c);
+                daaa[o] = (P[o] + t[tx][y]) * inv;
+            }
+        }
+        __syncthreads();
     }
 }
 
@@ -620,10 +679,55 @@ void launch_build_f(double *f, const double *aj, const double *atwo, int n, int 
     g_launches.fetch_add(1, std::memory_order_relaxed);
 }
 
-void launch_bro3(const Rdm &r, double *daaa, int nele, cudaStream_t st) {
-    ll n6 = (ll)r.n * r.n * r.n * r.n * r.n * r.n;
-    k_bro3<<<blocks_for(n6, 256), 256, 0, st>>>(r, daaa, 1.0 / (double)(nele - 3));
+// Column groups in an order that puts the permutations of one multiset
+// {ii,jj,kk} next to each other (they read the same ro4 columns).
+static void bro3_column_order(int n, std::vector<int> &ord) {
+    ord.clear();
+    for (int a = 0; a < n; ++a)
+        for (int b = a; b < n; ++b)
+            for (int c = b; c < n; ++c) {
+                const int v[3] = {a, b, c};
+                static const int P[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+                int seen[6], ns = 0;
+                for (auto &pp : P) {
+                    const int code = v[pp[0]] + n * (v[pp[1]] + n * v[pp[2]]);
+                    bool dup = false;
+                    for (int q = 0; q < ns; ++q) dup |= seen[q] == code;
+                    if (!dup) {
+                        seen[ns++] = code;
+                        ord.push_back(code);
+                    }
+                }
+            }
+}
+
+int launch_bro3(const Rdm &r, double *daaa, int nele, cudaStream_t st) {
+    const int n = r.n, M = r.M;
+    const ll n3 = (ll)n * n * n, n6 = n3 * n3;
+    std::vector<int> ord;
+    bro3_column_order(n, ord);
+    double *P = nullptr;
+    int *d_ord = nullptr;
+    if (cudaMallocAsync((void **)&P, sizeof(double) * 2 * (size_t)(M * n6), st) != cudaSuccess) return 2;
+    if (cudaMallocAsync((void **)&d_ord, sizeof(int) * ord.size(), st) != cudaSuccess) {
+        cudaFreeAsync(P, st);
+        return 2;
+    }
+    double *Q = P + (size_t)M * n6;
+    cudaMemcpyAsync(d_ord, ord.data(), sizeof(int) * ord.size(), cudaMemcpyHostToDevice, st);
+    ProfSpan span;
+    span.begin("bro3", st, 0);
+    for (int s0 = 0; s0 < M; s0 += kBro3States) {
+        k_bro3_case_a<<<(unsigned)n3, 256, 0, st>>>(r, d_ord, s0, std::min(kBro3States, M - s0), P, Q);
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+    }
+    dim3 g((unsigned)((n3 + 31) / 32), (unsigned)((n3 + 31) / 32));
+    k_bro3_combine<<<g, 256, 0, st>>>(P, Q, daaa, n3, M, 1.0 / (double)(nele - 3));
+    span.end();
     g_launches.fetch_add(1, std::memory_order_relaxed);
+    cudaFreeAsync(d_ord, st);
+    cudaFreeAsync(P, st);
+    return 0;
 }
 void launch_bro2(const Rdm &r, double *taa, int nele, cudaStream_t st) {
     ll n4 = (ll)r.n * r.n * r.n * r.n;

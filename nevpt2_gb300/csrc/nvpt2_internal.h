@@ -12,7 +12,8 @@ namespace nvpt {
 extern std::atomic<long long> g_launches;
 
 void launch_build_f(double *f, const double *aj, const double *atwo, int n, int ncore, int mode, cudaStream_t st);
-void launch_bro3(const Rdm &r, double *daaa, int nele, cudaStream_t st);
+// 0 on success, 2 if its scratch could not be allocated
+int launch_bro3(const Rdm &r, double *daaa, int nele, cudaStream_t st);
 void launch_bro2(const Rdm &r, double *taa, int nele, cudaStream_t st);
 void launch_bro1(const Rdm &r, double *dal, int nele, cudaStream_t st);
 void launch_aj_atwo(const double *oneint, const double *L, int Q, int n, int ncore, int norb, double *atwo,

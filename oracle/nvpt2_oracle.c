@@ -1297,3 +1297,32 @@ void orc_get_aj_atwo_twoint(const I *num, const I *indic, const I *jndic, const 
                         AIT(i + ncore, j + ncore, k + ncore, l + ncore);
 #undef AIT
 }
+
+/* Number of distinct packed 4-RDM entries bro3 (koopro4QD.F90:4881-4959)
+ * reads for one state: the algorithmic read volume of the partial trace. */
+I orc_bro3_touched(I nact) {
+    orc_ctx c;
+    o_init(&c, nact, 1);
+    const I n = nact, W = c.W, total = W * n * n * n * n;
+    unsigned char *seen = (unsigned char *)calloc((size_t)total, 1);
+    I count = 0;
+    for (I i = 1; i <= n; ++i)
+        for (I j = 1; j <= n; ++j)
+            for (I k = 1; k <= n; ++k)
+                for (I ii = 1; ii <= n; ++ii)
+                    for (I jj = 1; jj <= n; ++jj)
+                        for (I kk = 1; kk <= n; ++kk)
+                            for (I l = 1; l <= n; ++l) {
+                                I o[8];
+                                o_ord8(&c, i, j, k, l, ii, jj, kk, l, o);
+                                const I ind = o_lindice(&c, o[0], o[1], o[2], o[3]);
+                                const I a = (ind - 1) + W * ((o[4] - 1) + n * ((o[5] - 1) + n * ((o[6] - 1) + n * (o[7] - 1))));
+                                if (!seen[a]) {
+                                    seen[a] = 1;
+                                    ++count;
+                                }
+                            }
+    free(seen);
+    o_free(&c);
+    return count;
+}

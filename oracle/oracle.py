@@ -47,6 +47,8 @@ def lib():
         L.orc_bamat_slabs.argtypes = [P] * 7 + [I64, I64, P, P, I64, I64]
         L.orc_koop_matrices_ctl_sym.argtypes = [I64, I64, I64] + [P] * 15
         L.orc_bamat_sym.argtypes = [P] * 7 + [I64, I64, P, P, I64, P]
+        L.orc_bro3_touched.argtypes = [I64]
+        L.orc_bro3_touched.restype = I64
         L.orc_bamat_slab_list.argtypes = [P] * 7 + [I64, I64, P, P, I64, P, I64]
         L.orc_bbmat.argtypes = [P] * 6 + [I64, I64, P, P, I64]
         L.orc_bcmat.argtypes = [P] * 6 + [I64, I64, P, P, I64]
@@ -98,6 +100,11 @@ def bro3(ro4, nact, nele, metat):
     out = zeros(metat, *(nact,) * 6)
     lib().orc_bro3(_p(_chk(ro4)), _p(out), nact, nele, metat)
     return out
+
+
+def bro3_touched(nact):
+    """Distinct packed 4-RDM entries bro3 reads per state."""
+    return int(lib().orc_bro3_touched(nact))
 
 
 def bro2(daaa, nact, nele, metat):
