@@ -264,6 +264,14 @@ int nvpt_get_precision(nvpt_context *ctx);
 int nvpt_set_profiling(nvpt_context *ctx, int on);
 int nvpt_profile_read(nvpt_context *ctx, const char *tag, double *ms, int64_t *launches, int64_t *bytes);
 
+/* Polls a device-side wait (the grid barriers of the order-n^3 pencil
+ * tridiagonalisation, in nvpt_sytrd_d and nvpt_qdnevpt) makes before it
+ * gives up on ctx; 0 (the default) restores the built-in limit of 2^22
+ * polls with back-off (about 0.4 s).  A wait that gives up makes the kernel
+ * return, and the call returns NVPT_ETIMEDOUT with the context still usable.
+ * No counterpart in the reference; for callers that want a tighter bound. */
+int nvpt_set_wait_limit(nvpt_context *ctx, int64_t polls);
+
 /* Autotuning of launch parameters (no counterpart in the reference).  With
  * on = 1, the first call that meets a new shape of a tuned kernel times
  * every candidate of its parameter with CUDA events on the call's stream

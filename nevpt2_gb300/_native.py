@@ -88,6 +88,7 @@ _SIGS = {
     "nvpt_bcmat_d": ([P] + [P] * 6 + [I64, I64, P, P, I64, P], ctypes.c_int),
     "nvpt_bdmat_d": ([P] + [P] * 5 + [I64, I64, P, P, I64, P], ctypes.c_int),
     "nvpt_set_autotune": ([P, ctypes.c_int], ctypes.c_int),
+    "nvpt_set_wait_limit": ([P, I64], ctypes.c_int),
     "nvpt_autotune_report": ([P, ctypes.c_char_p, I64], I64),
     "nvpt_h5c_write": ([ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int],
                        ctypes.c_int),

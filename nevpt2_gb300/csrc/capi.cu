@@ -126,6 +126,7 @@ struct nvpt_context {
     std::string err;
     long long launches_at_create = 0;
     IjklState ijkl;
+    unsigned wait_limit = 0;  // nvpt_set_wait_limit (0 = built-in)
 };
 
 namespace {
@@ -283,6 +284,14 @@ const char *nvpt_context_error_set(nvpt_context *ctx, const char *msg) {
 }
 
 void *nvpt_context_stream(nvpt_context *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+unsigned nvpt_context_wait_limit(const nvpt_context *ctx) { return ctx ? ctx->wait_limit : 0u; }
+
+int nvpt_set_wait_limit(nvpt_context *ctx, int64_t polls) {
+    if (!ctx || polls < 0 || polls > 0xffffffffLL) return NVPT_EINVAL;
+    ctx->wait_limit = (unsigned)polls;
+    return NVPT_OK;
+}
 
 int64_t nvpt_launch_count(const nvpt_context *ctx) { return ctx ? g_launches.load() - ctx->launches_at_create : 0; }
 

@@ -28,6 +28,8 @@
 #include "../../include/nvpt2.h"
 #include "s2_tensor.cuh"
 
+extern "C" unsigned nvpt_context_wait_limit(const nvpt_context *ctx);
+
 namespace nvpt {
 namespace s2 {
 namespace {
@@ -1592,6 +1594,7 @@ struct ClassStreams {
             x.split = false;
             x.oz_err = nullptr;
             x.sm_share = 1;
+            x.wait_limit = 0;
         }
         CtxPool::release(c, dev);
     }
@@ -1731,6 +1734,7 @@ int run_qdnevpt(nvpt_context *ctx, cudaStream_t st, const nvpt_qdnevpt_in *in, n
             pc_.oz_err = c.oz_err;
             // measured: 8 pencils (4 states) fastest on quarters; 2 pencils on the whole GPU each
             pc_.sm_share = pc && pencils >= 4 ? 4 : 1;
+            pc_.wait_limit = nvpt_context_wait_limit(ctx);
         }
     ck(cudaEventRecord(ps.prep, c.st), "event");  // B and h ready
     std::vector<std::unique_ptr<Runner>> SR(M);

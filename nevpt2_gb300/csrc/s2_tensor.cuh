@@ -86,6 +86,9 @@ struct Ctx {
     // Order-n^3 pencils tridiagonalised at the same time on other streams:
     // each takes 1/sm_share of the SMs (at most 4), so that they overlap.
     int sm_share = 1;
+    // Polls a device-side wait (grid barrier) makes before it gives up and
+    // the call reports NVPT_ETIMEDOUT; 0 = the built-in limit.
+    unsigned wait_limit = 0;
 };
 
 T alloc(Ctx &c, std::initializer_list<long long> shape, bool zero = true);

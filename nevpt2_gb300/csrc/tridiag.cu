@@ -59,7 +59,7 @@ struct Bar {
 // next generation with a release store; the others poll the generation with
 // acquire loads.  Returns false if the wait timed out or another CTA
 // reported an error.
-__device__ bool grid_bar(Bar *b, unsigned nblk, unsigned &gen) {
+__device__ bool grid_bar(Bar *b, unsigned nblk, unsigned &gen, unsigned limit) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -75,7 +75,7 @@ __device__ bool grid_bar(Bar *b, unsigned nblk, unsigned &gen) {
             for (;;) {
                 asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(&b->gen) : "memory");
                 if (cur != g) break;
-                if (++spins > kBarSpin || *(volatile int *)&b->err) {
+                if (++spins > limit || *(volatile int *)&b->err) {
                     atomicExch(&b->err, 1);
                     ok = 0;
                     break;
@@ -111,6 +111,7 @@ struct PanelArgs {
     double *y;       // n
     double *acc;     // 2 x PARTS: the column sums (atomics), by column parity
     Bar *bar;
+    unsigned spin;   // polls before a barrier wait gives up
 };
 
 __global__ void __launch_bounds__(TT, 1) k_sytrd_panel(PanelArgs p) {
@@ -199,7 +200,7 @@ __global__ void __launch_bounds__(TT, 1) k_sytrd_panel(PanelArgs p) {
                 atomicAdd(acc + 3 + 2 * t, b);
             }
         }
-        if (!grid_bar(p.bar, G, gen)) return;
+        if (!grid_bar(p.bar, G, gen, p.spin)) return;
         // the other parity's sums were last read before this barrier: clear them for column j+1
         if (blockIdx.x == 0 && threadIdx.x < PARTS) accn[threadIdx.x] = 0.0;
         // ---- P2: the reflector of column j (every CTA forms the same scalars), v into shared memory
@@ -269,7 +270,7 @@ __global__ void __launch_bounds__(TT, 1) k_sytrd_panel(PanelArgs p) {
             s_tau_p = s_tau;
             s_beta_p = s_beta;
         }
-        if (!grid_bar(p.bar, G, gen)) return;
+        if (!grid_bar(p.bar, G, gen, p.spin)) return;
         pending = jj;
     }
     if (pending >= 0) finish(pending);
@@ -322,7 +323,7 @@ int sytrd_lower(Ctx &c, double *A, long long n, double *d, double *e, double *ta
     const double mone = -1.0, one = 1.0;
     for (long long j0 = 0; j0 < n; j0 += NBP) {
         const int nbp = (int)std::min<long long>(NBP, n - j0);
-        PanelArgs a{A, n, (int)j0, nbp, V.p, W.p, d, e, tau, y.p, accs.p, bar};
+        PanelArgs a{A, n, (int)j0, nbp, V.p, W.p, d, e, tau, y.p, accs.p, bar, c.wait_limit ? c.wait_limit : kBarSpin};
         void *args[] = {&a};
         ck(cudaLaunchCooperativeKernel((const void *)k_sytrd_panel, dim3(G), dim3(TT), args, vbytes, c.st),
            "cooperative launch");
@@ -348,6 +349,7 @@ int sytrd_lower(Ctx &c, double *A, long long n, double *d, double *e, double *ta
 // ===================================================================== C ABI
 extern "C" const char *nvpt_context_error_set(nvpt_context *ctx, const char *msg);
 extern "C" void *nvpt_context_stream(nvpt_context *ctx);
+extern "C" unsigned nvpt_context_wait_limit(const nvpt_context *ctx);
 
 extern "C" int nvpt_sytrd_d(nvpt_context *ctx, int64_t n, double *A, double *d, double *e, double *tau,
                             void *stream) {
@@ -364,6 +366,7 @@ extern "C" int nvpt_sytrd_d(nvpt_context *ctx, int64_t n, double *A, double *d, 
         if (!blas.h) ck(cublasCreate(&blas.h), "cublasCreate");
         ck(cublasSetStream(blas.h, st), "cublasSetStream");
         Ctx c{st, blas.h, nullptr};
+        c.wait_limit = nvpt_context_wait_limit(ctx);
         const int rc = sytrd_lower(c, A, n, d, e, tau, false);
         if (rc) {
             nvpt_context_error_set(ctx, "sytrd: a grid barrier timed out");

@@ -56,3 +56,40 @@ def test_sytrd_reflectors_rebuild_the_matrix(n):
     T = np.diag(d) + np.diag(e, 1) + np.diag(e, -1)
     assert np.abs(Q @ T @ Q.T - A).max() <= 1e-13 * n * np.abs(A).max()
     assert np.abs(Q.T @ Q - np.eye(n)).max() <= 1e-13 * n
+
+
+def test_barrier_timeout_reports_and_the_context_recovers():
+    """A grid-barrier wait that runs out of polls makes the kernel return and
+    the call report NVPT_ETIMEDOUT; the context stays usable.  The limit of
+    one poll makes every CTA that is not the last to arrive give up."""
+    torch = pytest.importorskip("torch")
+    from nevpt2_gb300._native import Context, NvptError
+    n = 512
+    A = _sym(n, 5)
+    dev = torch.device("cuda:0")
+    ctx = Context(0)
+    d = torch.zeros(n, dtype=torch.float64, device=dev)
+    e = torch.zeros(n, dtype=torch.float64, device=dev)
+    tau = torch.zeros(n, dtype=torch.float64, device=dev)
+    ctx.call("nvpt_set_wait_limit", 1)
+    statuses = []
+    for _ in range(3):
+        tA = torch.from_numpy(A.ravel(order="F").copy()).to(dev)
+        try:
+            ctx.call("nvpt_sytrd_d", n, ptr(tA), ptr(d), ptr(e), ptr(tau), None)
+            ctx.synchronize()
+            statuses.append(0)
+        except NvptError as err:
+            statuses.append(err.status)
+            if err.status == 5:
+                break
+    assert statuses[-1] == 5, statuses
+    ctx.call("nvpt_set_wait_limit", 0)
+    tA = torch.from_numpy(A.ravel(order="F").copy()).to(dev)
+    ctx.call("nvpt_sytrd_d", n, ptr(tA), ptr(d), ptr(e), ptr(tau), None)
+    ctx.synchronize()
+    linalg = pytest.importorskip("scipy.linalg")
+    w = linalg.eigh_tridiagonal(d.cpu().numpy(), e.cpu().numpy()[:n - 1], eigvals_only=True)
+    ref = np.linalg.eigvalsh(A)
+    assert np.abs(np.sort(w) - ref).max() <= 50 * n * 2.2e-16 * np.abs(ref).max()
+    ctx.close()
