@@ -512,11 +512,12 @@ int launch_bamat_gemm(const Rdm &r, const double *atwo, const double *f, int nco
         if (rrc) return 3;
     }
     AsyncBuffers buf(st);
-    double *A1, *A2, *A3, *T, *X;
+    double *A1, *A2, *A3, *T, *X[2];
     const int B = slabs_per_batch;
     int *slabs;
     if (!buf.get(&A1, sizeof(double) * 3 * n4) || !buf.get(&T, sizeof(double) * 4 * n6) ||
-        !buf.get(&X, sizeof(double) * 4 * (size_t)B * n6) || !buf.get(&slabs, sizeof(int) * 2 * n * n))
+        !buf.get(&X[0], sizeof(double) * 4 * (size_t)B * n6) || !buf.get(&X[1], sizeof(double) * 4 * (size_t)B * n6) ||
+        !buf.get(&slabs, sizeof(int) * 2 * n * n))
         return 2;
     A2 = A1 + n4;
     A3 = A2 + n4;
@@ -526,34 +527,80 @@ int launch_bamat_gemm(const Rdm &r, const double *atwo, const double *f, int nco
     int rc = 0;
     // split precision: digit workspace for a full batch of slabs
     void *ozw = nullptr;
-    unsigned long long *rmax = nullptr;  // row maxima of the four slab layouts (split digits)
+    unsigned long long *rmax[2] = {nullptr, nullptr};  // row maxima of the four slab layouts (split digits)
     if (split) {
         oz::OzPlan pl(4, (ll)B * n3, (int)n3, n);
-        if (!buf.get(&ozw, pl.bytes()) || !buf.get(&rmax, sizeof(unsigned long long) * 4 * (size_t)B * n3)) return 2;
+        if (!buf.get(&ozw, pl.bytes()) || !buf.get(&rmax[0], sizeof(unsigned long long) * 4 * (size_t)B * n3) ||
+            !buf.get(&rmax[1], sizeof(unsigned long long) * 4 * (size_t)B * n3))
+            return 2;
     }
-    for (int s = 0; s < M && !rc; ++s) {
-        for (int s0 = 0; s0 < n * n && !rc; s0 += B) {
-            int nb = std::min(B, n * n - s0);
-            double *X1 = X, *X2 = X + (ll)B * n6, *X3 = X2 + (ll)B * n6, *X4 = X3 + (ll)B * n6;
-            ll rows = (ll)nb * n3;
-            if (rmax) cudaMemsetAsync(rmax, 0, sizeof(unsigned long long) * 4 * (size_t)rows, st);
-            k_bamat_slabs_t<<<(unsigned)rows, 256, 0, st>>>(r, s, slabs + s0, slabs + n * n + s0, nb, X1, X2,
-                                                                   X3, X4, rmax);
-            g_launches.fetch_add(1, std::memory_order_relaxed);
-            double *T1 = T + (ll)s0 * n4, *T2 = T + n6 + (ll)s0 * n4, *T3 = T + 2 * n6 + (ll)s0 * n4,
-                   *T4 = T + 3 * n6 + (ll)s0 * n4;
-            if (split) {
-                const double *Xs[4] = {X1, X2, X3, X4}, *As[4] = {A1, A2, A3, A3};
-                double *Ts[4] = {T1, T2, T3, T4};
-                const unsigned long long *Rm[4] = {rmax, rmax + rows, rmax + 2 * rows, rmax + 3 * rows};
-                rc |= oz::oz_gemm_skinny(oz::OzPlan(4, rows, (int)n3, n), Xs, As, Ts, n, n, ozw, st, Rm);
-                continue;
+    // Slab production (gather-bound on the packed 4-RDM) runs one batch ahead
+    // on a stream of its own into the other of two slab buffers, so that it
+    // overlaps the products of the current batch (FP64 pipe, or HBM-bound
+    // digit streams in split mode).  Events order buffer reuse; the guard
+    // joins the producer stream into st before the buffers are released
+    // (it is destroyed before `buf`).
+    struct Producer {
+        cudaStream_t st, g = nullptr;
+        cudaEvent_t in = nullptr, gen[2] = {nullptr, nullptr}, use[2] = {nullptr, nullptr}, end = nullptr;
+        bool ok = false;
+        explicit Producer(cudaStream_t s) : st(s) {
+            ok = cudaStreamCreateWithFlags(&g, cudaStreamNonBlocking) == cudaSuccess;
+            for (cudaEvent_t *e : {&in, &gen[0], &gen[1], &use[0], &use[1], &end})
+                ok = ok && cudaEventCreateWithFlags(e, cudaEventDisableTiming) == cudaSuccess;
+            ok = ok && cudaEventRecord(in, st) == cudaSuccess && cudaStreamWaitEvent(g, in, 0) == cudaSuccess;
+        }
+        ~Producer() {
+            if (g && end) {
+                cudaEventRecord(end, g);
+                cudaStreamWaitEvent(st, end, 0);
             }
-            const double *Xs[4] = {X1, X2, X3, X4}, *As[4] = {A1, A2, A3, A3};
-            double *Ts[4] = {T1, T2, T3, T4};
+            for (cudaEvent_t e : {in, gen[0], gen[1], use[0], use[1], end})
+                if (e) cudaEventDestroy(e);
+            if (g) cudaStreamDestroy(g);
+        }
+    } prod(st);
+    if (!prod.ok) return 1;
+    const int per_state = (n * n + B - 1) / B, nbatch = M * per_state;
+    auto batch = [&](int gb, int &s, int &s0, int &nb) {
+        s = gb / per_state;
+        s0 = (gb % per_state) * B;
+        nb = std::min(B, n * n - s0);
+    };
+    auto produce = [&](int gb) {
+        int s, s0, nb;
+        batch(gb, s, s0, nb);
+        const int q = gb & 1;
+        if (gb >= 2) cudaStreamWaitEvent(prod.g, prod.use[q], 0);
+        const ll rows = (ll)nb * n3;
+        double *X1 = X[q], *X2 = X1 + (ll)B * n6, *X3 = X2 + (ll)B * n6, *X4 = X3 + (ll)B * n6;
+        if (rmax[q]) cudaMemsetAsync(rmax[q], 0, sizeof(unsigned long long) * 4 * (size_t)rows, prod.g);
+        k_bamat_slabs_t<<<(unsigned)rows, 256, 0, prod.g>>>(r, s, slabs + s0, slabs + n * n + s0, nb, X1, X2, X3, X4,
+                                                             rmax[q]);
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+        cudaEventRecord(prod.gen[q], prod.g);
+    };
+    produce(0);
+    for (int gb = 0; gb < nbatch && !rc; ++gb) {
+        if (gb + 1 < nbatch) produce(gb + 1);
+        int s, s0, nb;
+        batch(gb, s, s0, nb);
+        const int q = gb & 1;
+        cudaStreamWaitEvent(st, prod.gen[q], 0);
+        const ll rows = (ll)nb * n3;
+        double *X1 = X[q], *X2 = X1 + (ll)B * n6, *X3 = X2 + (ll)B * n6, *X4 = X3 + (ll)B * n6;
+        double *T1 = T + (ll)s0 * n4, *T2 = T + n6 + (ll)s0 * n4, *T3 = T + 2 * n6 + (ll)s0 * n4,
+               *T4 = T + 3 * n6 + (ll)s0 * n4;
+        const double *Xs[4] = {X1, X2, X3, X4}, *As[4] = {A1, A2, A3, A3};
+        double *Ts[4] = {T1, T2, T3, T4};
+        if (split) {
+            const unsigned long long *Rm[4] = {rmax[q], rmax[q] + rows, rmax[q] + 2 * rows, rmax[q] + 3 * rows};
+            rc |= oz::oz_gemm_skinny(oz::OzPlan(4, rows, (int)n3, n), Xs, As, Ts, n, n, ozw, st, Rm);
+        } else {
             rc |= dgemm_skinny4(st, rows, n, (int)n3, Xs, As, Ts);
         }
-        if (!rc) {
+        cudaEventRecord(prod.use[q], st);
+        if (!rc && s0 + nb == n * n) {  // last batch of state s
             k_bamat_assemble<<<(unsigned)((n6 + 255) / 256), 256, 0, st>>>(n, M, s, T, T + n6, T + 2 * n6, T + 3 * n6,
                                                                         amat, atmat);
             g_launches.fetch_add(1, std::memory_order_relaxed);
