@@ -374,6 +374,14 @@ typedef struct {
     double *e2mpp, *psimpp, *e2enp, *psienep;
     double *e2mp, *e2en, *psimp, *psien, *epsnew;
     int64_t *nnew;
+    /* .NATORB (compute_rho1st): the first-order density blocks of the PC
+     * classes in the canonical orbitals, Fortran order with the state last:
+     * rhoir (ncore, nvirt, metat) from (0') (src/qdnevpt.F:4971), rhoid
+     * (ncore, nact, metat) from (+1') (:5187), rhodr (nact, nvirt, metat)
+     * from (-1') (:5407).  Any non-NULL pointer makes the call form all three;
+     * the reference writes them to its RHOFILE and assembles the density at
+     * :1240-1300. */
+    double *rhoir, *rhoid, *rhodr;
 } nvpt_qdnevpt_out;
 
 /* src/qdnevpt.F:858-993, the per-state loop of qdnevpt (integral transforms,

@@ -168,8 +168,13 @@ __global__ void k_pc_finish(const double *R, const double *Rp, const double *Rj,
 // shared memory; one thread runs the elimination and the back substitution
 // there (every step a shared-memory access, no global latency), then all
 // threads form the dot products.  Shared memory: 6 n doubles.
+// With nd > 0 the kernel also forms rho[l nd + k] = -x . Y[:, dcol0 + k] for
+// k < nd: the first-order density of the label against nd extra right-hand
+// sides transformed with the labels' (sum_mu r_mu v_mu,k / (w_mu + sig) =
+// z^T (K + sig S)^-1 g_k with v = C^T g).
 __global__ void k_tridiag_resolvent(const double *d, const double *e, long long n, const double *Y, long long ncol,
-                                    long long L, int nother, const double *sig, double *acc) {
+                                    long long L, int nother, const double *sig, double *acc, int nd,
+                                    long long dcol0, double *rho) {
     extern __shared__ double sm[];
     double *sd = sm, *se = sm + n, *wb = sm + 2 * n, *wc = sm + 3 * n, *wd = sm + 4 * n, *wy = sm + 5 * n;
     const long long l = blockIdx.x;
@@ -225,6 +230,24 @@ __global__ void k_tridiag_resolvent(const double *d, const double *e, long long 
     block_add(en, acc + 0);
     block_add(ps, acc + 1);
     for (int j = 0; j < nother && j < 8; ++j) block_add(offs[j], acc + 2 + j);
+    for (int k = 0; k < nd; ++k) {
+        double r = 0.0;
+        for (long long i = threadIdx.x; i < n; i += blockDim.x) r -= Y[i * ncol + dcol0 + k] * wy[i];
+        block_add(r, rho + l * nd + k);
+    }
+}
+
+// First-order density of a PC class on its eigenpairs: rho[l, k] =
+// -sum_mu R[l, mu] V[k, mu] / (w_mu + base_l), one thread per (l, k).
+__global__ void k_rho_pc(const double *R, const double *V, const double *w, const double *base, long long L,
+                         long long nmu, int nd, double *rho) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= L * nd) return;
+    const long long l = t / nd;
+    const int k = (int)(t % nd);
+    double acc = 0.0;
+    for (long long mu = 0; mu < nmu; ++mu) acc -= R[l * nmu + mu] * V[(long long)k * nmu + mu] / (w[mu] + base[l]);
+    rho[t] = acc;
 }
 
 // v0 (class 0): labels (ii <= ij) x (r <= s); G[i,r,j,s] = (i r | j s) wait: G = Rcv^T Rcv
@@ -480,9 +503,20 @@ struct Accum {  // host mirror of the reference's energy holders
     int M;
     std::vector<double> e2mpp, psimpp, e2enp, psienep, e2mp, e2en, psimp, psien;
     std::vector<long long> nnew;
-    Accum(int m)
+    // first-order density blocks (compute_rho1st), Fortran order with the
+    // state last: rhoir (nc, nv, M), rhoid (nc, na, M), rhodr (na, nv, M)
+    bool rho = false;
+    int nc = 0, na = 0, nv = 0;
+    std::vector<double> rhoir, rhoid, rhodr;
+    Accum(int m, int nc_ = 0, int na_ = 0, int nv_ = 0, bool rho_ = false)
         : M(m), e2mpp(8 * m), psimpp(8 * m), e2enp(8 * m), psienep(8 * m), e2mp(m * m), e2en(m * m), psimp(m),
-          psien(m), nnew(10 * m, -1) {}
+          psien(m), nnew(10 * m, -1), rho(rho_), nc(nc_), na(na_), nv(nv_) {
+        if (rho) {
+            rhoir.assign((size_t)nc * nv * m, 0.0);
+            rhoid.assign((size_t)nc * na * m, 0.0);
+            rhodr.assign((size_t)na * nv * m, 0.0);
+        }
+    }
     double &E(std::vector<double> &v, int cls, int s) { return v[cls + 8 * s]; }   // (8, M) column-major
     double &H(std::vector<double> &v, int j, int s) { return v[j + M * s]; }       // (M, M) column-major
     // Adds the contributions a class collected in its own (zero-started)
@@ -494,6 +528,9 @@ struct Accum {  // host mirror of the reference's energy holders
         };
         add(e2mpp, o.e2mpp); add(psimpp, o.psimpp); add(e2enp, o.e2enp); add(psienep, o.psienep);
         add(e2mp, o.e2mp); add(e2en, o.e2en); add(psimp, o.psimp); add(psien, o.psien);
+        if (rho && o.rho) {
+            add(rhoir, o.rhoir); add(rhoid, o.rhoid); add(rhodr, o.rhodr);
+        }
         for (size_t i = 0; i < nnew.size(); ++i)
             if (o.nnew[i] != -1) nnew[i] = o.nnew[i];
     }
@@ -692,7 +729,8 @@ class Runner {
     }
     // PC sums from the tridiagonal form of a pencil: Yt row-major [n][M L]
     // (column k L + l: state block k of label l), shifts per label.
-    std::vector<double> resolvent_sums(const PencilTridiag &PT, const T &Yt, const std::vector<double> &shift) {
+    std::vector<double> resolvent_sums(const PencilTridiag &PT, const T &Yt, const std::vector<double> &shift,
+                                       int nd = 0, long long dcol0 = 0, double *rho = nullptr) {
         const long long L = (long long)shift.size(), n = PT.n;
         T sg = upload(c, shift);
         T a = alloc(c, {2 + 8}, true);
@@ -704,11 +742,23 @@ class Runner {
             ProfSpan sp;
             sp.begin("pencil_solve", c.st, 0);
             k_tridiag_resolvent<<<(unsigned)L, 128, smem, c.st>>>(PT.d.p, PT.e.p, n, Yt.p, Yt.sh[1], L, M - 1, sg.p,
-                                                                   a.p);
+                                                                   a.p, nd, dcol0, rho);
             sp.end();
             LAUNCHED();
         }
         return download(c, a.p, 2 + 8);
+    }
+    // First-order density on the eigenpairs: [L, nd] = -sum_mu R[l,mu] V[k,mu] / (w_mu + base_l)
+    std::vector<double> rho_pc(const T &R, const T &V, const T &w, const std::vector<double> &base, long long nmu,
+                               int nd) {
+        const long long L = (long long)base.size();
+        T bs = upload(c, base);
+        T out = alloc(c, {L, (long long)nd}, true);
+        if (L * nd > 0) {
+            k_rho_pc<<<nblk(L * nd), TPB, 0, c.st>>>(R.p, V.p, w.p, bs.p, L, nmu, nd, out.p);
+            LAUNCHED();
+        }
+        return download(c, out.p, L * nd);
     }
     void pc_accum(std::vector<double> &e2, double &psi2, const std::vector<double> &r) {
         e2[s + M * s] += r[0];
@@ -1291,6 +1341,16 @@ class Runner {
         double psi2 = 0.0;
         pc_accum(e2, psi2, pc_finish(R, nullptr, Rj, nullptr, P.w, pb, n2, 0));
         pc_store(7, e2, psi2, true);
+        if (acc.rho) {
+            // e20pcont :4854-4860, :4971-4975: rhoir(i,r) -= sum_mu c_mu vaux_mu with
+            // vaux_mu = sum_ab da(a,b) (2 coef(ab,mu) - coef(ab+nn,mu))
+            T v = alloc(c, {1, n2}, false);
+            gemm(c, false, false, 1, n2, nn, 2.0, D.g1.p, nn, Ctop.p, n2, 0.0, v.p, n2);
+            gemm(c, false, false, 1, n2, nn, -1.0, D.g1.p, nn, Cbot.p, n2, 1.0, v.p, n2);
+            auto rl = rho_pc(R, v, P.w, pb, n2, 1);
+            for (int i = 0; i < nc; ++i)
+                for (int r = 0; r < nv; ++r) acc.rhoir[i + (size_t)nc * (r + (size_t)nv * s)] += rl[(size_t)i * nv + r];
+        }
     }
 
     // ------------------------------------------------ classes (-1') and (+1')
@@ -1465,6 +1525,29 @@ class Runner {
         for (long long l = 0; l < L; ++l) pb[l] = -base[l];
         std::vector<double> e2(M * M, 0.0);
         double psi2 = 0.0;
+        // compute_rho1st: vaux(d,mu) = sum_abc coef(mu,abc) g_d[abc] with g_d[abc] =
+        // ee2(d,b,a,c) for (-1') (e2m1pcont :5326-5343, into rhodr) and ee2tl(d,b,a,c)
+        // for (+1') (e21pcont :5113-5125, into rhoid); rho -= sum_mu c_mu vaux(d,mu)
+        const int nd = acc.rho ? n : 0;
+        T Ed;
+        if (nd) {
+            Ed = alloc(c, {(long long)n, (long long)n3}, false);
+            if (minus) {
+                permute(c, E2.p, {n, n, n, n}, {0, 2, 1, 3}, Ed.p);
+            } else {
+                T E2tl = alloc(c, {n, n, n, n}, false);
+                build_ee2tlL(c, E2.p, D.g1.p, n, E2tl.p);
+                permute(c, E2tl.p, {n, n, n, n}, {0, 2, 1, 3}, Ed.p);
+            }
+        }
+        auto store_rho = [&](const std::vector<double> &rl) {
+            for (long long l = 0; l < L; ++l)
+                for (int d = 0; d < n; ++d) {
+                    const double v = rl[(size_t)l * n + d];
+                    if (minus) acc.rhodr[d + (size_t)na * (l + (size_t)nv * s)] += v;
+                    else acc.rhoid[l + (size_t)nc * (d + (size_t)na * s)] += v;
+                }
+        };
         PencilTridiag PT;
         if (n3 >= kPcCholMin && metric_above(c, S.p, n3, thr) && pencil_tridiag(c, K.p, S.p, n3, PT)) {
             // Every metric eigenvalue is kept (nnew = n3): the PC sums over
@@ -1472,14 +1555,21 @@ class Runner {
             //   sum_mu r_mu^2 / (w_mu + s) = z^T (K + s S)^-1 z,
             // evaluated in the pencil's tridiagonal form (no eigenvectors).
             acc.nnew[(minus ? 7 : 6) + 10 * s] = (int)n3;
-            T Z = alloc(c, {(long long)M, L, (long long)n3}, false);  // own state, then the others
+            // own state, then the others, then the nd density vectors g_d
+            T Z = alloc(c, {(long long)M * L + nd, (long long)n3}, false);
             zm(S, W2t, Z.p);
             auto o = others();
             for (size_t k = 0; k < o.size(); ++k) other_z(o[k], Z.p + (long long)(k + 1) * L * n3);
-            pencil_rhs(c, PT, Z.p, (long long)M * L);  // rows of Z are the columns of a column-major [n3, M L]
-            Z = view2(std::move(Z), (long long)M * L, n3);
-            T Yt = permuted(c, Z, {1, 0});  // [n3][M L]
-            pc_accum(e2, psi2, resolvent_sums(PT, Yt, pb));
+            if (nd)
+                ck(cudaMemcpyAsync(Z.p + (long long)M * L * n3, Ed.p, sizeof(double) * nd * n3,
+                                   cudaMemcpyDeviceToDevice, c.st), "cp");
+            // rows of Z are the columns of a column-major [n3, M L + nd]
+            pencil_rhs(c, PT, Z.p, (long long)M * L + nd);
+            Z = view2(std::move(Z), (long long)M * L + nd, n3);
+            T Yt = permuted(c, Z, {1, 0});  // [n3][M L + nd]
+            T rho = alloc(c, {L, (long long)(nd ? nd : 1)}, true);
+            pc_accum(e2, psi2, resolvent_sums(PT, Yt, pb, nd, (long long)M * L, rho.p));
+            if (nd) store_rho(download(c, rho.p, L * nd));
         } else {
             PcResult P = pc_transform(c, S, K, n3, thr);
             acc.nnew[(minus ? 7 : 6) + 10 * s] = P.nnew;
@@ -1493,6 +1583,11 @@ class Runner {
                 gemm(c, false, false, L, n3, n3, 1.0, Z.p, n3, P.C.p, n3, 0.0, out, n3);
             });
             pc_accum(e2, psi2, pc_finish(R, nullptr, Rj, nullptr, P.w, pb, n3, 0));
+            if (nd) {
+                T V = alloc(c, {(long long)nd, (long long)n3}, false);
+                gemm(c, false, false, nd, n3, n3, 1.0, Ed.p, n3, P.C.p, n3, 0.0, V.p, n3);
+                store_rho(rho_pc(R, V, P.w, pb, n3, nd));
+            }
         }
         pc_store(minus ? 6 : 5, e2, psi2, true);
     }
@@ -1689,7 +1784,9 @@ int run_qdnevpt(nvpt_context *ctx, cudaStream_t st, const nvpt_qdnevpt_in *in, n
             pd[k].d3 = fortran_slice(c, T3, P, k, n, 6);
         }
     }
-    Accum acc(M);
+    // compute_rho1st: the first-order density blocks when the caller asks for them
+    const bool want_rho = out->rhoir || out->rhoid || out->rhodr;
+    Accum acc(M, nc, na, nv, want_rho);
     Runner R(c, nc, na, nv, M, Q, in->thr_lindep, in->frozen, sd, pd, acc);
     {
         T chol = S(in->cholesky_array, Q * npair);
@@ -1765,7 +1862,7 @@ int run_qdnevpt(nvpt_context *ctx, cudaStream_t st, const nvpt_qdnevpt_in *in, n
         for (int k = 0; k < norb; ++k) epsnew[k + (size_t)norb * st_] = SR[st_]->eps[k];
     {
         const size_t nt = (size_t)M * nj;
-        std::vector<Accum> local(nt, Accum(M));
+        std::vector<Accum> local(nt, Accum(M, nc, na, nv, want_rho));
         std::vector<std::exception_ptr> fail(nt);
         auto work = [&](size_t idx) {
             const size_t st_ = idx / nj, k = idx % nj;
@@ -1812,6 +1909,9 @@ int run_qdnevpt(nvpt_context *ctx, cudaStream_t st, const nvpt_qdnevpt_in *in, n
     put(out->psienep, acc.psienep); put(out->e2mp, acc.e2mp); put(out->e2en, acc.e2en);
     put(out->psimp, acc.psimp); put(out->psien, acc.psien); put(out->epsnew, epsnew);
     if (out->nnew) std::memcpy(out->nnew, acc.nnew.data(), sizeof(int64_t) * acc.nnew.size());
+    if (want_rho) {
+        put(out->rhoir, acc.rhoir); put(out->rhoid, acc.rhoid); put(out->rhodr, acc.rhodr);
+    }
     return NVPT_OK;
 }
 

@@ -33,7 +33,7 @@ class _In(ctypes.Structure):
 
 class _Out(ctypes.Structure):
     _fields_ = [("e2mpp", P), ("psimpp", P), ("e2enp", P), ("psienep", P), ("e2mp", P), ("e2en", P),
-                ("psimp", P), ("psien", P), ("epsnew", P), ("nnew", P)]
+                ("psimp", P), ("psien", P), ("epsnew", P), ("nnew", P), ("rhoir", P), ("rhoid", P), ("rhodr", P)]
 
 
 @dataclass
@@ -48,6 +48,10 @@ class Stage2Energies:
     psien: np.ndarray
     epsnew: np.ndarray
     nnew: np.ndarray
+    # first-order density blocks (rho1st=True): (ncore,nvirt,M), (ncore,nact,M), (nact,nvirt,M)
+    rhoir: np.ndarray | None = None
+    rhoid: np.ndarray | None = None
+    rhodr: np.ndarray | None = None
 
 
 _BOUND = False
@@ -74,10 +78,11 @@ def _f(a):
 
 
 def qdnevpt(problem, koop: dict, transition=None, thr_lindep: float = 1e-6, class_mask: int = 0xFF,
-            no_pc: bool = False, frozen=None) -> Stage2Energies:
+            no_pc: bool = False, frozen=None, rho1st: bool = False) -> Stage2Energies:
     """Per-state loop of src/qdnevpt.F:858-993 on the GPU.  ``koop`` holds
     the stage-1 datasets by their nevpt.h5 names; ``transition`` the
-    (1-TRDM, 2-TRDM, 3-TRDM) arrays when metat > 1."""
+    (1-TRDM, 2-TRDM, 3-TRDM) arrays when metat > 1; ``rho1st`` (.NATORB)
+    also returns the first-order density blocks of the PC classes."""
     ctx = context()
     _bind(ctx)
     p = problem
@@ -106,10 +111,48 @@ def qdnevpt(problem, koop: dict, transition=None, thr_lindep: float = 1e-6, clas
     res = Stage2Energies(*(np.zeros((8, M), order="F") for _ in range(4)), np.zeros((M, M), order="F"),
                          np.zeros((M, M), order="F"), np.zeros(M), np.zeros(M), np.zeros((p.norb, M), order="F"),
                          np.zeros((10, M), np.int64, order="F"))
-    out = _Out(*(ptr(getattr(res, k)) for k in ("e2mpp", "psimpp", "e2enp", "psienep", "e2mp", "e2en", "psimp",
-                                                  "psien", "epsnew", "nnew")))
+    if rho1st:
+        nc, nv = p.ncore, p.nvirt
+        res.rhoir = np.zeros((nc, nv, M), order="F")
+        res.rhoid = np.zeros((nc, n, M), order="F")
+        res.rhodr = np.zeros((n, nv, M), order="F")
+    names = ("e2mpp", "psimpp", "e2enp", "psienep", "e2mp", "e2en", "psimp", "psien", "epsnew", "nnew", "rhoir",
+             "rhoid", "rhodr")
+    out = _Out(*(ptr(getattr(res, k)) for k in names))
     ctx.check(ctx._lib.nvpt_qdnevpt(ctx.handle, ctypes.byref(inp), ctypes.byref(out)), "nvpt_qdnevpt")
     return res
+
+
+def natural_orbitals(res: Stage2Energies, dal, ncore: int, nact: int, nvirt: int):
+    """src/qdnevpt.F:1240-1411 (.NATORB) on the host: each state's density in
+    the canonical orbitals (2 on the inactive diagonal, the 1-RDM on the
+    active block, the PC classes' first-order blocks off the diagonal,
+    symmetric) and its natural occupation numbers (dsyev, then the
+    reference's order_eigvalvec, :1484: descending magnitude, a later value of
+    equal magnitude first).  Returns (rho (norb, norb, M), occupations (norb, M))."""
+    if res.rhoir is None:
+        raise ValueError("run qdnevpt(..., rho1st=True) first")
+    M = res.rhoir.shape[2]
+    norb = ncore + nact + nvirt
+    c, a, v = slice(0, ncore), slice(ncore, ncore + nact), slice(ncore + nact, norb)
+    rho = np.zeros((norb, norb, M))
+    occ = np.zeros((norb, M))
+    for s in range(M):
+        R = rho[:, :, s]
+        R[a, a] = np.asarray(dal)[s]
+        R[np.arange(ncore), np.arange(ncore)] = 2.0
+        for blk, rs, cs in ((res.rhoir, c, v), (res.rhodr, a, v), (res.rhoid, c, a)):
+            R[rs, cs] = blk[:, :, s]
+            R[cs, rs] = blk[:, :, s].T
+        w = np.linalg.eigvalsh(np.tril(R) + np.tril(R, -1).T)
+        for i in range(norb - 1):
+            imin = i
+            for j in range(i + 1, norb):
+                if abs(w[j]) >= abs(w[imin]):
+                    imin = j
+            w[i], w[imin] = w[imin], w[i]
+        occ[:, s] = w
+    return rho, occ
 
 
 @dataclass

@@ -237,6 +237,12 @@ class Stage2Result:
     psien: np.ndarray
     nnew: dict          # PC metric ranks per class and state
     epsnew: np.ndarray  # (norb, M)
+    # first-order density blocks of the PC classes (compute_rho1st):
+    # rhoir (0') inactive-virtual, rhoid (+1') inactive-active, rhodr (-1')
+    # active-virtual, each (rows, cols, M) in the canonical orbitals
+    rhoir: np.ndarray | None = None
+    rhoid: np.ndarray | None = None
+    rhodr: np.ndarray | None = None
 
 
 class _State:
@@ -308,7 +314,8 @@ def qdnevpt(inp: Stage2Inputs, classes=range(8), pc=True, timings: dict | None =
     h = unpack_tri(inp.oneint, norb)
     r = Stage2Result(e2mpp=np.zeros((8, M)), psimpp=np.zeros((8, M)), e2enp=np.zeros((8, M)),
                      psienep=np.zeros((8, M)), e2mp=np.zeros((M, M)), e2en=np.zeros((M, M)), psimp=np.zeros(M),
-                     psien=np.zeros(M), nnew={}, epsnew=np.zeros((norb, M)))
+                     psien=np.zeros(M), nnew={}, epsnew=np.zeros((norb, M)), rhoir=np.zeros((nc, nv, M)),
+                     rhoid=np.zeros((nc, na, M)), rhodr=np.zeros((na, nv, M)))
     fro = np.zeros(norb, bool)
     for k in inp.frozen:
         fro[k] = True
@@ -897,6 +904,8 @@ def _v0pmod(inp, st, s, r, fro, pc):
     psi2 = 0.0
     ev = eps[virt]
     gba = g1.T.reshape(nn)  # da(b,a) at [ab]
+    # e20pcont :4854-4860: vaux(mu) = sum_ab da(a,b) (2 coef(ab,mu) - coef(ab+nn,mu))
+    vaux = 2.0 * (g1.reshape(nn) @ C[:nn]) - g1.reshape(nn) @ C[nn:]
     for i in range(nc):
         if fro[i]:
             continue
@@ -915,6 +924,7 @@ def _v0pmod(inp, st, s, r, fro, pc):
             cir = co / deno
             e2[s, s] -= (co * cir).sum()
             psi2 += (cir ** 2).sum()
+            r.rhoir[i, irv, s] -= (cir * vaux).sum()  # :4971-4975
             for k in rim:
                 if k != s:
                     e2[k, s] -= (rim[k] * rim[s] / deno).sum()
@@ -1013,6 +1023,8 @@ def _vmupE(inp, st, s, r, fro, pc):
         sm[j] = (So @ C, np.transpose(W2o, (3, 0, 1, 2)).reshape(n, n3) @ C)
     e2 = np.zeros((M, M))
     psi2 = 0.0
+    # e2m1pcont :5326-5343: vaux(d,mu) = sum_abc coef(mu,abc) ee2(d,b,a,c)
+    vaux = np.transpose(E2, (0, 2, 1, 3)).reshape(n, n3) @ C
     for irv in range(nv):
         d = X3[:, :, :, irv]
         rabc = np.transpose(d, (0, 2, 1)).reshape(n3)  # dint1(a,c,b) at abc (c fastest)
@@ -1022,6 +1034,7 @@ def _vmupE(inp, st, s, r, fro, pc):
         co = rm[s] / deno
         e2[s, s] -= (rm[s] * co).sum()
         psi2 += (co ** 2).sum()
+        r.rhodr[:, irv, s] -= vaux @ co  # :5407-5411
         for k in rm:
             if k != s:
                 e2[k, s] -= (rm[s] * (rm[k] / deno)).sum()
@@ -1122,6 +1135,8 @@ def _vpupE(inp, st, s, r, fro, pc):
         sm[j] = (So @ C, np.transpose(W2o, (3, 0, 1, 2)).reshape(n, n3) @ C)
     e2 = np.zeros((M, M))
     psi2 = 0.0
+    # e21pcont :5113-5125: vaux(d,mu) = sum_abc coef(mu,abc) ee2tl(d,b,a,c)
+    vaux = np.transpose(ee2tlL(E2, g1), (0, 2, 1, 3)).reshape(n, n3) @ C
     for ii in range(nc):
         if fro[ii]:
             continue
@@ -1133,6 +1148,7 @@ def _vpupE(inp, st, s, r, fro, pc):
         co = am[s] / deno
         e2[s, s] -= (am[s] * co).sum()
         psi2 += (co ** 2).sum()
+        r.rhoid[ii, :, s] -= vaux @ co  # :5187-5191
         for k in am:
             if k != s:
                 e2[k, s] -= (am[s] * (am[k] / deno)).sum()
@@ -1203,3 +1219,44 @@ def heff_qd(e2, energies):
     w, evc, info = sla.lapack.dsyev(Hh, compute_v=1, lower=0)
     assert info == 0
     return wr, wi, vr, Hh, evc, w
+
+
+def first_order_density(r: Stage2Result, dal, ncore: int, nact: int, nvirt: int):
+    """src/qdnevpt.F:1240-1300 (.NATORB): the density of every state in the
+    canonical orbitals -- 2 on the inactive diagonal, the 1-RDM on the active
+    block, the PC classes' first-order blocks (inactive-virtual from (0'),
+    active-virtual from (-1'), inactive-active from (+1')), symmetric.
+    Returns rho (norb, norb, M).  (The reference reads these blocks back from
+    a file that its (0') routine rewinds for every state, which keeps one
+    state's records; per state they are the quantities formed here.)"""
+    M = r.rhoir.shape[2]
+    norb = ncore + nact + nvirt
+    rho = np.zeros((norb, norb, M))
+    c, a, v = slice(0, ncore), slice(ncore, ncore + nact), slice(ncore + nact, norb)
+    for s in range(M):
+        rho[a, a, s] = dal[s]
+        rho[np.arange(ncore), np.arange(ncore), s] = 2.0
+        rho[c, v, s] = r.rhoir[:, :, s]
+        rho[v, c, s] = r.rhoir[:, :, s].T
+        rho[a, v, s] = r.rhodr[:, :, s]
+        rho[v, a, s] = r.rhodr[:, :, s].T
+        rho[c, a, s] = r.rhoid[:, :, s]
+        rho[a, c, s] = r.rhoid[:, :, s].T
+    return rho
+
+
+def natural_occupations(rho_s):
+    """:1400-1411: dsyev('V','L') of one state's density, then
+    order_eigvalvec (:1484): a selection sort by descending magnitude in which
+    a later value of equal magnitude wins."""
+    w = sla.eigh(np.tril(rho_s) + np.tril(rho_s, -1).T, lower=True, eigvals_only=True).copy()
+    m = w.size
+    for i in range(m - 1):
+        emin, imin = w[i], i
+        for j in range(i + 1, m):
+            if abs(w[j]) >= abs(emin):
+                emin, imin = w[j], j
+        if imin != i:
+            w[imin] = w[i]
+            w[i] = emin
+    return w
