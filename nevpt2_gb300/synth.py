@@ -256,6 +256,8 @@ def with_ci(p: Problem, amask, bmask, coef) -> Problem:
 CONFIGS = {
     "cas8": dict(nact=8, nele=8, ncore=10, nvirt=40, metat=1, ndet=None, seed=20261203 + 1),
     "cas14": dict(nact=14, nele=14, ncore=20, nvirt=150, metat=1, ndet=50_000, seed=20261203 + 2),
+    # a mid-size case for single-kernel profiler captures (slab buffers above L2, a few GB in all)
+    "cas10": dict(nact=10, nele=10, ncore=10, nvirt=40, metat=1, ndet=20_000, seed=20261203 + 10),
     "cas16_qd4": dict(nact=16, nele=16, ncore=30, nvirt=250, metat=4, ndet=100_000, seed=20261203 + 5),
 }
 

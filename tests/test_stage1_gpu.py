@@ -144,4 +144,4 @@ def test_launch_counter_moves(gpu_ctx):
     before = gpu_ctx.launches
     p = synth.make_problem(4, 4, 1, 2, seed=3)
     koopro.bro3(p.ro4, 4, 4, 1)
-    assert gpu_ctx.launches == before + 1
+    assert gpu_ctx.launches == before + 2  # bro3: the case-A pass and the transpose-add
