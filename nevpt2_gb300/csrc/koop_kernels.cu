@@ -66,16 +66,35 @@ __global__ void __launch_bounds__(256) k_bro3_case_a(Rdm r, const int *col_order
     const ll n3 = (ll)n * n * n;
     const int c = col_order[blockIdx.x];
     const int ii = c % n + 1, jj = (c / n) % n + 1, kk = c / (n * n) + 1;
+    __shared__ int s_n2[16];  // normind(ii,jj,kk,l) per l
+    if (threadIdx.x < n) s_n2[threadIdx.x] = normind4(ii, jj, kk, threadIdx.x + 1);
+    __syncthreads();
     for (ll rr = threadIdx.x; rr < n3; rr += blockDim.x) {
         const int i = (int)(rr % n) + 1, j = (int)((rr / n) % n) + 1, k = (int)(rr / ((ll)n * n)) + 1;
         double p[kBro3States], q[kBro3States];
 #pragma unroll
         for (int t = 0; t < kBro3States; ++t) p[t] = q[t] = 0.0;
         for (int l = 1; l <= n; ++l) {
-            const int n1 = normind4(i, j, k, l), n2 = normind4(ii, jj, kk, l);
+            // ord8 with the first group as key (case A): its selection sort,
+            // the same swaps on the partner; lindice of the sorted key is
+            // normind of the first group
+            int kq[4] = {i, j, k, l}, pq[4] = {ii, jj, kk, l};
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                int imax = kq[a], jmax = a;
+#pragma unroll
+                for (int b = a + 1; b < 4; ++b)
+                    if (kq[b] > imax) { imax = kq[b]; jmax = b; }
+#pragma unroll
+                for (int b = a + 1; b < 4; ++b)  // static indices: the arrays stay in registers
+                    if (jmax == b) {
+                        int t = kq[a]; kq[a] = kq[b]; kq[b] = t;
+                        t = pq[a]; pq[a] = pq[b]; pq[b] = t;
+                    }
+            }
+            const int n1 = lindice4(kq[0], kq[1], kq[2], kq[3]), n2 = s_n2[l - 1];
             if (n1 < n2) continue;
-            int q0, q1, q2, q3;
-            const int ind = ord8_key(i, j, k, l, ii, jj, kk, l, q0, q1, q2, q3);
+            const int ind = n1, q0 = pq[0], q1 = pq[1], q2 = pq[2], q3 = pq[3];
 #pragma unroll
             for (int t = 0; t < kBro3States; ++t) {
                 if (t >= ns) break;
@@ -85,10 +104,12 @@ __global__ void __launch_bounds__(256) k_bro3_case_a(Rdm r, const int *col_order
             }
         }
         const ll o = (ll)M * (rr + n3 * c);
-        for (int t = 0; t < ns; ++t) {
-            P[o + s0 + t] = p[t];
-            Q[o + s0 + t] = q[t];
-        }
+#pragma unroll
+        for (int t = 0; t < kBro3States; ++t)
+            if (t < ns) {
+                P[o + s0 + t] = p[t];
+                Q[o + s0 + t] = q[t];
+            }
     }
 }
 
