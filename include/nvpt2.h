@@ -232,6 +232,28 @@ int nvpt_read_rdm_from_resfile(nvpt_context *ctx, const char *path, int which, i
 int nvpt_read_distributed_rdm(nvpt_context *ctx, const char *dir, const char *result_name, int which, int trans,
                               double *rdm, int64_t ld, int64_t nact, int64_t total_elements);
 
+/* Spin-free RDMs of a determinant-expanded CI vector, on the device (the
+ * role of src/koopro4QD.F90:921 rofour, :1571 ro3, :2412 ro2, :2861 ro1 and
+ * the transition variants ro3off :1978, ro2off :2620, ro1off :2936, for CI
+ * vectors given as determinant lists).  Determinant I is the bitmask pair
+ * amask[I], bmask[I] (bit p = active orbital p occupied), creators in
+ * ascending spin-orbital order with all alpha before all beta; coef is
+ * (ndet, nroot) column-major; all pointers are device pointers.
+ * nvpt_rdm_dense_d adds the k-RDM (k = 1, 2, 3) of bra root s and ket root t
+ * to out[slot + ldo (P1 + n P2 + ... + n^(2k-1) Q_k)] -- the reference's
+ * dal/taa/daaa(s,...) layouts with ldo = metat, slot = the state (or the
+ * pair index for transition matrices): dal(i,j) = <E_ij>, taa(i,j,k,l) =
+ * sum <a+_i a+_j a_l a_k>, daaa(i,j,k,l,m,n) = sum <a+_i a+_j a+_k a_n a_m a_l>.
+ * nvpt_rofour_d adds the packed 4-RDM of root s to ro4_s (W x n^4, the
+ * state's slice of ro4), every slot (ind(K), L) with normind(L) <=
+ * normind(K); other slots are not touched.  Both read out/ro4_s, so the
+ * caller zeroes them first. */
+int nvpt_rdm_dense_d(nvpt_context *ctx, int64_t nact, int64_t k, int64_t ndet, const uint32_t *amask,
+                     const uint32_t *bmask, const double *coef, int64_t nroot, int64_t s, int64_t t, double *out,
+                     int64_t ldo, int64_t slot, void *stream);
+int nvpt_rofour_d(nvpt_context *ctx, int64_t nact, int64_t ndet, const uint32_t *amask, const uint32_t *bmask,
+                  const double *coef, int64_t nroot, int64_t s, double *ro4_s, void *stream);
+
 /* Precision of the dense contractions of later calls on ctx (no counterpart
  * in the reference).  NVPT_PRECISION_FP64 (the default) is the drop-in.
  * NVPT_PRECISION_SPLIT runs the n^9 slab products of bamat, and in

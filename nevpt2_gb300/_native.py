@@ -98,6 +98,8 @@ _SIGS = {
     "nvpt_read_rdm_from_resfile": ([P, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, P, I64, I64, P], ctypes.c_int),
     "nvpt_read_distributed_rdm": ([P, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, P, I64, I64,
                                    I64], ctypes.c_int),
+    "nvpt_rdm_dense_d": ([P, I64, I64, I64, P, P, P, I64, I64, I64, P, I64, I64, P], ctypes.c_int),
+    "nvpt_rofour_d": ([P, I64, I64, P, P, P, I64, I64, P, P], ctypes.c_int),
     "nvpt_ijkl_init": ([P, I64, P, P, P, P], ctypes.c_int),
     "nvpt_ijkl_tables": ([P] + [P] * 8, ctypes.c_int),
     "nvpt_ijkl_set_twoint": ([P, P], ctypes.c_int),

@@ -21,7 +21,7 @@ CSRC = PKG / "csrc"
 INCLUDE = PKG.parent / "include"
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
-CUDA_SOURCES = ["capi.cu", "koop_kernels.cu", "bamat.cu", "bamat_gemm.cu", "s2_tensor.cu", "tridiag.cu", "qdnevpt.cu", "ozaki.cu", "ozaki_wide.cu", "rdm_unfold.cu", "ijkl_sym.cu", "tuner.cu", "container.cpp"]
+CUDA_SOURCES = ["capi.cu", "koop_kernels.cu", "bamat.cu", "bamat_gemm.cu", "s2_tensor.cu", "tridiag.cu", "qdnevpt.cu", "ozaki.cu", "ozaki_wide.cu", "rdm_unfold.cu", "ijkl_sym.cu", "tuner.cu", "container.cpp", "rdm_build.cu"]
 CUDA_HEADERS = ["eexx.cuh", "nvpt2_internal.h", "s2_tensor.cuh", "ozaki.cuh", "oz_ptx.cuh", "tuner.h"]
 
 

@@ -396,6 +396,35 @@ int nvpt_get_aj_atwo_d(nvpt_context *ctx, double *atwo, int64_t nact, int64_t nc
     return after_launch(ctx, "get_aj_atwo");
 }
 
+// ------------------------------------------------ RDMs of a CI expansion
+static int rdm_args(nvpt_context *ctx, int64_t nact, int64_t ndet, int64_t nroot, int64_t s, int64_t t) {
+    if (!ctx) return NVPT_EINVAL;
+    if (nact < 1 || nact > 16) return fail(ctx, NVPT_EINVAL, "rdm: nact must be in [1,16]");
+    if (ndet < 1 || ndet >= (1LL << 31)) return fail(ctx, NVPT_EINVAL, "rdm: ndet must be in [1, 2^31)");
+    if (nroot < 1 || s < 0 || s >= nroot || t < 0 || t >= nroot) return fail(ctx, NVPT_EINVAL, "rdm: bad root");
+    return NVPT_OK;
+}
+
+int nvpt_rdm_dense_d(nvpt_context *ctx, int64_t nact, int64_t k, int64_t ndet, const uint32_t *amask,
+                     const uint32_t *bmask, const double *coef, int64_t nroot, int64_t s, int64_t t, double *out,
+                     int64_t ldo, int64_t slot, void *stream) {
+    NV_TRY(rdm_args(ctx, nact, ndet, nroot, s, t));
+    if (k < 1 || k > 3) return fail(ctx, NVPT_EINVAL, "rdm_dense: k must be 1, 2 or 3");
+    if (ldo < 1 || slot < 0 || slot >= ldo) return fail(ctx, NVPT_EINVAL, "rdm_dense: bad ldo/slot");
+    const int rc = launch_rdm_dense((int)nact, (int)k, ndet, amask, bmask, coef, (int)s, (int)t, out, ldo, slot,
+                                    pick(ctx, stream));
+    if (rc == 2) return fail(ctx, NVPT_ENOMEM, "rdm_dense: device allocation failed");
+    return after_launch(ctx, "rdm_dense");
+}
+
+int nvpt_rofour_d(nvpt_context *ctx, int64_t nact, int64_t ndet, const uint32_t *amask, const uint32_t *bmask,
+                  const double *coef, int64_t nroot, int64_t s, double *ro4_s, void *stream) {
+    NV_TRY(rdm_args(ctx, nact, ndet, nroot, s, s));
+    const int rc = launch_rofour((int)nact, ndet, amask, bmask, coef, (int)s, ro4_s, pick(ctx, stream));
+    if (rc == 2) return fail(ctx, NVPT_ENOMEM, "rofour: device allocation failed");
+    return after_launch(ctx, "rofour");
+}
+
 // ------------------------------------------------ symmetry-packed integrals
 int nvpt_ijkl_init(nvpt_context *ctx, int64_t nsym, const int64_t *nish, const int64_t *nash, const int64_t *nssh,
                    int64_t *ni4) {

@@ -60,6 +60,13 @@ void launch_ai_twoint(const IjklTables &T, long long count, const int64_t *ijkl,
 void launch_sym_screen(double *x, double *y, int M, int n, int k, const long long *irr, cudaStream_t st);
 void launch_aj_atwo_twoint(const IjklTables &T, const double *oneint, int n, int ncore, int norb, double *atwo,
                            double *aj, cudaStream_t st);
+// Spin-free RDMs of a determinant expansion (rdm_build.cu): dense k <= 3 for
+// (bra s, ket t) accumulated at out[slot + ldo (P + n^k Q)]; packed 4-RDM of
+// root s.  0 on success, 2 on an allocation failure.
+int launch_rdm_dense(int n, int k, long long ndet, const unsigned *amask, const unsigned *bmask, const double *coef,
+                     int s, int t, double *out, long long ldo, long long slot, cudaStream_t st);
+int launch_rofour(int n, long long ndet, const unsigned *amask, const unsigned *bmask, const double *coef, int s,
+                  double *ro4_s, cudaStream_t st);
 // Kernel spans for live measurement (nvpt_set_profiling): when enabled, a
 // tagged launch is bracketed by CUDA events on its stream together with its
 // algorithmic byte count; nvpt_profile_read sums the spans of one tag.

@@ -221,6 +221,54 @@ def rdms(n: int, amask, bmask, coef, with_ro4: bool = True):
     return dal, taa, daaa, ro4
 
 
+def rdms_device(n: int, amask, bmask, coef, with_ro4: bool = True, transition: bool = False, ctx=None,
+                device: str = "cuda:0"):
+    """The outputs of ``rdms`` (and, with transition=True, of
+    ``transition_rdms`` as a fifth item) computed on the GPU by the library's
+    RDM builder (nvpt_rdm_dense_d / nvpt_rofour_d), returned as host arrays."""
+    import torch
+
+    from ._native import Context, ptr
+    ctx = ctx or Context(torch.device(device).index or 0)
+    dev = torch.device(device)
+    coef = np.asfortranarray(coef, dtype=np.float64)
+    nd, M = coef.shape
+    am = torch.from_numpy(np.ascontiguousarray(amask, dtype=np.uint32).view(np.int32)).to(dev)
+    bm = torch.from_numpy(np.ascontiguousarray(bmask, dtype=np.uint32).view(np.int32)).to(dev)
+    cf = torch.from_numpy(coef.ravel(order="F").copy()).to(dev)
+    z = lambda k: torch.zeros(k, dtype=torch.float64, device=dev)
+    outs = [z(M * n ** (2 * k)) for k in (1, 2, 3)]
+    for s in range(M):
+        for k, o in zip((1, 2, 3), outs):
+            ctx.call("nvpt_rdm_dense_d", n, k, nd, ptr(am), ptr(bm), ptr(cf), M, s, s, ptr(o), M, s, None)
+    ro4 = None
+    W = nwords(n)
+    if with_ro4:
+        r4 = z(W * n**4 * M)
+        for s in range(M):
+            ctx.call("nvpt_rofour_d", n, nd, ptr(am), ptr(bm), ptr(cf), M, s, ctypes.c_void_p(r4.data_ptr() + 8 * W * n**4 * s),
+                     None)
+    tr = None
+    if transition and M > 1:
+        P = M * (M - 1) // 2
+        tr_d = [z(P * n ** (2 * k)) for k in (1, 2, 3)]
+        for big in range(M):
+            for small in range(big):
+                kp = big * (big - 1) // 2 + small
+                for k, o in zip((1, 2, 3), tr_d):
+                    ctx.call("nvpt_rdm_dense_d", n, k, nd, ptr(am), ptr(bm), ptr(cf), M, small, big, ptr(o), P, kp,
+                             None)
+    ctx.synchronize()
+    host = lambda t, shape: t.cpu().numpy().reshape(shape, order="F")
+    dal, taa, daaa = (host(o, (M,) + (n,) * (2 * k)) for k, o in zip((1, 2, 3), outs))
+    if with_ro4:
+        ro4 = host(r4, (W,) + (n,) * 4 + (M,))
+    if transition and M > 1:
+        P = M * (M - 1) // 2
+        tr = [host(o, (P,) + (n,) * (2 * k)) for k, o in zip((1, 2, 3), tr_d)]
+    return (dal, taa, daaa, ro4, tr) if transition else (dal, taa, daaa, ro4)
+
+
 def transition_rdms(n: int, amask, bmask, coef):
     """Transition 1-3-RDMs for every root pair (big > small), stored at pair
     index big*(big-1)/2 + small (the reference's iroot > jroot loop,
