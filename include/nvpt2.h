@@ -402,7 +402,9 @@ typedef struct {
      * (ncore, nact, metat) from (+1') (:5187), rhodr (nact, nvirt, metat)
      * from (-1') (:5407).  Any non-NULL pointer makes the call form all three;
      * the reference writes them to its RHOFILE and assembles the density at
-     * :1240-1300. */
+     * :1240-1300.  The canonical orbitals' signs are the device eigensolver's
+     * choice: a block's row or column may differ in sign from another
+     * eigensolver's result, the density's eigenvalues do not. */
     double *rhoir, *rhoid, *rhodr;
 } nvpt_qdnevpt_out;
 

@@ -26,6 +26,7 @@
 #include <cublas_v2.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <atomic>
 #include <vector>
 
@@ -429,7 +430,87 @@ __global__ void __launch_bounds__(256, 2) k_dgemm_skinny(SkinnyJobs jobs, ll row
     }
 }
 
+// The same product on the FP64 tensor cores: mma.sync m8n8k4 (DMMA).  CTA
+// tile 128 x 16 as above (X staged transposed, B as [k][16] in shared
+// memory); warp w owns rows 16w .. 16w+15 as two 8-row blocks times two 8-col
+// blocks, four accumulators of two doubles per lane.  Fragments (PTX m8n8k4
+// .f64): A a0 = A[lane/4][lane%4], B b0 = B[lane%4][lane/4], C c0,c1 =
+// C[lane/4][2(lane%4) + {0,1}].
+__global__ void __launch_bounds__(256, 2) k_dgemm_skinny_dmma(SkinnyJobs jobs, ll rows, int N, int K) {
+    constexpr int BM = 128, LD = BM + 1, NX = BM / 8;
+    __shared__ double Xs[kSkBK * LD];
+    __shared__ __align__(16) double Bs[kSkBK * 16];
+    const int jb = blockIdx.y;
+    const double *__restrict__ X = jb == 0 ? jobs.X[0] : jb == 1 ? jobs.X[1] : jb == 2 ? jobs.X[2] : jobs.X[3];
+    const double *__restrict__ B = jb == 0 ? jobs.B[0] : jb == 1 ? jobs.B[1] : jb == 2 ? jobs.B[2] : jobs.B[3];
+    double *__restrict__ C = jb == 0 ? jobs.C[0] : jb == 1 ? jobs.C[1] : jb == 2 ? jobs.C[2] : jobs.C[3];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const ll r0 = (ll)blockIdx.x * BM;
+    const int lk = tid & 31, lr = tid >> 5;
+    double xr[NX], br[2];
+    auto load = [&](int k0) {
+        const int k = k0 + lk;
+#pragma unroll
+        for (int i = 0; i < NX; ++i) {
+            const ll r = r0 + lr + 8 * i;
+            xr[i] = (r < rows && k < K) ? X[r * K + k] : 0.0;
+        }
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            const int e = tid + 256 * i, kk = e >> 4, c = e & 15;
+            br[i] = (c < N && k0 + kk < K) ? B[(ll)(k0 + kk) * N + c] : 0.0;
+        }
+    };
+    double acc[2][2][2] = {};  // [m block][n block][c0, c1]
+    const int g = lane >> 2, q = lane & 3;
+    load(0);
+    for (int k0 = 0; k0 < K; k0 += kSkBK) {
+#pragma unroll
+        for (int i = 0; i < NX; ++i) Xs[lk * LD + lr + 8 * i] = xr[i];
+#pragma unroll
+        for (int i = 0; i < 2; ++i) Bs[tid + 256 * i] = br[i];
+        __syncthreads();
+        if (k0 + kSkBK < K) load(k0 + kSkBK);
+#pragma unroll
+        for (int kk = 0; kk < kSkBK; kk += 4) {
+            double a[2], b[2];
+#pragma unroll
+            for (int mb = 0; mb < 2; ++mb) a[mb] = Xs[(kk + q) * LD + warp * 16 + mb * 8 + g];
+#pragma unroll
+            for (int nb = 0; nb < 2; ++nb) b[nb] = Bs[(kk + q) * 16 + nb * 8 + g];
+#pragma unroll
+            for (int mb = 0; mb < 2; ++mb)
+#pragma unroll
+                for (int nb = 0; nb < 2; ++nb)
+                    asm volatile(
+                        "mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
+                        : "+d"(acc[mb][nb][0]), "+d"(acc[mb][nb][1])
+                        : "d"(a[mb]), "d"(b[nb]));
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int mb = 0; mb < 2; ++mb) {
+        const ll r = r0 + warp * 16 + mb * 8 + g;
+        if (r >= rows) continue;
+#pragma unroll
+        for (int nb = 0; nb < 2; ++nb)
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const int col = nb * 8 + 2 * q + i;
+                if (col < N) C[r * N + col] = acc[mb][nb][i];
+            }
+    }
+}
+
+// variant: 2, 4 = DFMA register blocks of 2 or 4 rows per thread; 1 = DMMA
 static void launch_skinny(int rpt, cudaStream_t st, const SkinnyJobs &j, ll rows, int N, int K) {
+    if (rpt == 1) {
+        dim3 grid((unsigned)((rows + 127) / 128), 4);
+        k_dgemm_skinny_dmma<<<grid, 256, 0, st>>>(j, rows, N, K);
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+        return;
+    }
     const ll bm = 32LL * rpt;
     dim3 grid((unsigned)((rows + bm - 1) / bm), 4);
     if (rpt == 2) k_dgemm_skinny<2><<<grid, 256, 0, st>>>(j, rows, N, K);
@@ -446,11 +527,22 @@ static int dgemm_skinny4(cudaStream_t st, ll rows, int N, int K, const double *c
         j.C[i] = C[i];
     }
     // rows per thread (tile height 32 RPT), tuned per shape
-    static const int kRpt[] = {2, 4};
+    // variant, tuned per shape: DFMA with 2 or 4 rows per thread, or DMMA;
+    // NVPT_SKINNY_VARIANT (1, 2, 4) fixes it (tests of each variant)
+    static const int kRpt[] = {2, 4, 1};
+    static const int forced = [] {
+        const char *e = std::getenv("NVPT_SKINNY_VARIANT");
+        const int v = e ? std::atoi(e) : 0;
+        return (v == 1 || v == 2 || v == 4) ? v : 0;
+    }();
+    if (forced) {
+        launch_skinny(forced, st, j, rows, N, K);
+        return cudaPeekAtLastError() == cudaSuccess ? 0 : 1;
+    }
     const std::string key = "bamat_skinny.rows_per_thread/" + std::to_string(rows) + "x" + std::to_string(K) + "x" +
                             std::to_string(N);
     int used = -1;
-    const int rpt = tune::choose(key, kRpt, 2, 4, st, [&](int c) { launch_skinny(c, st, j, rows, N, K); used = c; });
+    const int rpt = tune::choose(key, kRpt, 3, 4, st, [&](int c) { launch_skinny(c, st, j, rows, N, K); used = c; });
     if (used < 0) launch_skinny(rpt, st, j, rows, N, K);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : 1;
 }
