@@ -62,6 +62,9 @@ def _args():
     ap.add_argument("--parity", action="store_true",
                     help="compare the FP64 and split energies with the oracle's stage 2 fed the GPU's FP64 Koopmans "
                          "matrices, per class and in total, with the split error split between stage 1 and stage 2")
+    ap.add_argument("--parity-dump", metavar="NPZ",
+                    help="with --parity: save the GPU's FP64 2-HRDM, 2-EAKO, orbital energies and class energies "
+                         "(the inputs of oracle.extended_pc --inputs)")
     ap.add_argument("--oz-gemm", nargs=3, type=int, metavar=("ROWS", "K", "N"),
                     help="time the split-precision product kernel alone on a random ROWS x K by K x N problem")
     return ap.parse_args()
@@ -748,6 +751,9 @@ def run_parity(args):
     stage1(koopro.FP64)
     e64 = stage2(koopro.FP64)
     koop64 = {k: st.result(k) for k in st.out}
+    if args.parity_dump:
+        np.savez(args.parity_dump, hrdm=koop64["2-HRDM"], eako2=koop64["2-EAKO"], epsnew=np.asarray(e64.epsnew),
+                 e2enp=np.asarray(e64.e2enp), e2mpp=np.asarray(e64.e2mpp))
 
     # FP64 noise floor of every class: the stage-2 energies after one relative
     # rounding (2^-52 xi, xi ~ N(0,1)) of every element of its inputs (all

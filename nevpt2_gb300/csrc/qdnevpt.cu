@@ -748,6 +748,28 @@ class Runner {
         }
         return download(c, a.p, 2 + 8);
     }
+    // The resolvent route of a PC class whose metric keeps every eigenvalue
+    // (nnew = nd): sum_mu r_mu^2 / (w_mu + s_l) = z_l^T (K + s_l S)^-1 z_l.
+    // fill(Z) writes the numerator rows z before the PC basis change, Z
+    // row-major [M L, nd]: own state first, then the other states in
+    // others() order.  Returns false, with nothing accumulated and fill not
+    // called, when a metric eigenvalue is below the threshold.
+    bool pc_resolvent(const T &S, const T &K, long long nd, long long L, int nnew_slot,
+                      const std::vector<double> &shift, std::vector<double> &e2, double &psi2,
+                      const std::function<void(double *)> &fill) {
+        if (nd == 0 || L == 0) return false;
+        PencilTridiag PT;
+        if (!(metric_above(c, S.p, nd, thr) && pencil_tridiag(c, K.p, S.p, nd, PT))) return false;
+        acc.nnew[nnew_slot + 10 * s] = (int)nd;
+        const long long rows = (long long)M * L;
+        T Z = alloc(c, {rows, nd}, false);
+        fill(Z.p);
+        // rows of Z are the columns of a column-major [nd, M L]
+        pencil_rhs(c, PT, Z.p, rows);
+        T Yt = permuted(c, Z, {1, 0});  // [nd][M L]
+        pc_accum(e2, psi2, resolvent_sums(PT, Yt, shift));
+        return true;
+    }
     // First-order density on the eigenpairs: [L, nd] = -sum_mu R[l,mu] V[k,mu] / (w_mu + base_l)
     std::vector<double> rho_pc(const T &R, const T &V, const T &w, const std::vector<double> &base, long long nmu,
                                int nd) {
@@ -1091,17 +1113,14 @@ class Runner {
         // ---- (a) r != s: metric fillcm2 (row (i,j), j fastest) ----
         {
             T S = copy_of(c, Dm.p, {n2, n2}), K = copy_of(c, Km.p, {n2, n2});
-            PcResult P = pc_transform(c, S, K, n2, thr);
-            acc.nnew[(plus ? 2 : 4) + 10 * s] = P.nnew;
-            T sm = matmul(c, S, true, P.C, false);  // s(ab,mu) = sum_{pq} D[pq,ab] C[pq,mu]
             // labels: plus (i<j core): dint[ab] = (i b | j a) = T[i,b,j,a];
             //         minus (r<s virt): dint[ab] = d1(b,a), d1 = (r a | s b) -> T[b,r,a,s]
             PairGather g = plus ? PairGather{0, st0, st2, 0, st3, st1, N, 1, n, n, 1, 1.0, 0.0, 0.0}
                                 : PairGather{0, st1, st3, 0, st2, st0, N, 1, n, n, 1, 1.0, 0.0, 0.0};
             T V = pair_gather(c, Tm, g);
             zero_rows(V, fne);
-            T R = matmul(c, V, false, sm, false);
-            T Rj = stack_others(Lne, n2, [&](int j, double *out) {
+            // the transition metric of another state j, [(ap,bp), (a,b)]
+            auto xmet = [&](int j) {
                 auto [PD, lt] = off(j);
                 T rt = alloc(c, {n, n, n, n}, false);
                 if (plus) build_ro2toff(c, PD->d2.p, PD->d1.p, n, rt.p);
@@ -1109,13 +1128,32 @@ class Runner {
                 // plus: lt rt^(1,0,3,2) else rt^(3,2,1,0); minus: lt d^(3,2,1,0) else d^(1,0,3,2)
                 bool a1 = plus ? lt : !lt;
                 T X = a1 ? permuted(c, rt, {1, 0, 3, 2}) : permuted(c, rt, {3, 2, 1, 0});
-                T Xm = view2(std::move(X), n2, n2);
-                T sj = matmul(c, Xm, false, P.C, false);
-                gemm(c, false, false, Lne, n2, n2, 1.0, V.p, n2, sj.p, n2, 0.0, out, n2);
-            });
+                return view2(std::move(X), n2, n2);
+            };
             std::vector<double> pb(Lne);  // deno = w - eps_i - eps_j  /  w + eps_r + eps_s
             for (long long l = 0; l < Lne; ++l) pb[l] = -bne[l];
-            pc_accum(e2, psi2, pc_finish(R, nullptr, Rj, nullptr, P.w, pb, n2, 0));
+            // numerators before the PC basis change: own z = S^T v (R = V S^T C), other z = X_j^T v
+            const bool res = pc_resolvent(S, K, n2, Lne, plus ? 2 : 4, pb, e2, psi2, [&](double *Z) {
+                gemm(c, false, true, Lne, n2, n2, 1.0, V.p, n2, S.p, n2, 0.0, Z, n2);
+                auto o = others();
+                for (size_t k = 0; k < o.size(); ++k) {
+                    T Xm = xmet(o[k]);
+                    gemm(c, false, false, Lne, n2, n2, 1.0, V.p, n2, Xm.p, n2, 0.0, Z + (long long)(k + 1) * Lne * n2,
+                         n2);
+                }
+            });
+            if (!res) {
+                PcResult P = pc_transform(c, S, K, n2, thr);
+                acc.nnew[(plus ? 2 : 4) + 10 * s] = P.nnew;
+                T sm = matmul(c, S, true, P.C, false);  // s(ab,mu) = sum_{pq} D[pq,ab] C[pq,mu]
+                T R = matmul(c, V, false, sm, false);
+                T Rj = stack_others(Lne, n2, [&](int j, double *out) {
+                    T Xm = xmet(j);
+                    T sj = matmul(c, Xm, false, P.C, false);
+                    gemm(c, false, false, Lne, n2, n2, 1.0, V.p, n2, sj.p, n2, 0.0, out, n2);
+                });
+                pc_accum(e2, psi2, pc_finish(R, nullptr, Rj, nullptr, P.w, pb, n2, 0));
+            }
         }
         // ---- (b) r == s: metric fillcm2p on pairs a <= b ----
         {
@@ -1125,11 +1163,6 @@ class Runner {
             T Kf = copy_of(c, Km.p, {n2, n2});
             permute(c, Km.p, {n, n, n, n}, {0, 1, 3, 2}, Kf.p, 1.0, true);
             T Sp = restrict_sq(Sf), Kp = restrict_sq(Kf);
-            PcResult P = pc_transform(c, Sp, Kp, np, thr);
-            acc.nnew[(plus ? 3 : 5) + 10 * s] = P.nnew;
-            // s(ab,mu) = sum_{abp} 0.5 Sf[abp, ab] C[abp, mu]
-            T smp = matmul(c, Sp, true, P.C, false);
-            axpby(c, np * np, 0.5, smp.p, 0.0, nullptr, smp.p);
             // labels: plus core i: dint[pair(a,b)] = w T[i,b,i,a]; minus virt r: w T[a,r,b,r]
             T Vf = alloc(c, {(long long)N, (long long)n2}, false);
             if (plus) gather(c, Tm.p, 0, {N, n, n}, {st0 + st2, st3, st1}, Vf.p);  // [i, a, b] = T[i,b,i,a]
@@ -1137,8 +1170,8 @@ class Runner {
             zero_rows(Vf, feq);
             T Pw = pair_matrix(1.0, 2.0, false);
             T V = matmul(c, Vf, false, Pw, false);  // [N, np]
-            T R = matmul(c, V, false, smp, false);
-            T Rj = stack_others(Leq, np, [&](int j, double *out) {
+            // the transition metric of another state j on pairs, [pair ab, pair abp]
+            auto xmet = [&](int j) {
                 auto [PD, lt] = off(j);
                 T rt = alloc(c, {n, n, n, n}, false);
                 if (plus) build_ro2toff(c, PD->d2.p, PD->d1.p, n, rt.p);
@@ -1154,13 +1187,34 @@ class Runner {
                     permute(c, rt.p, {n, n, n, n}, {3, 2, 1, 0}, X.p, 0.5, false);
                     permute(c, rt.p, {n, n, n, n}, {3, 2, 0, 1}, X.p, 0.5, true);
                 }
-                T Xr = restrict_sq(X);  // [pair ab, pair abp]
-                T sj = matmul(c, Xr, false, P.C, false);
-                gemm(c, false, false, Leq, np, np, 1.0, V.p, np, sj.p, np, 0.0, out, np);
-            });
+                return restrict_sq(X);
+            };
             std::vector<double> pb(Leq);
             for (long long l = 0; l < Leq; ++l) pb[l] = -beq[l];
-            pc_accum(e2, psi2, pc_finish(R, nullptr, Rj, nullptr, P.w, pb, np, 0));
+            // numerators before the PC basis change: own z = 0.5 Sp^T v, other z = X_j^T v
+            const bool res = pc_resolvent(Sp, Kp, np, Leq, plus ? 3 : 5, pb, e2, psi2, [&](double *Z) {
+                gemm(c, false, true, Leq, np, np, 0.5, V.p, np, Sp.p, np, 0.0, Z, np);
+                auto o = others();
+                for (size_t k = 0; k < o.size(); ++k) {
+                    T Xr = xmet(o[k]);
+                    gemm(c, false, false, Leq, np, np, 1.0, V.p, np, Xr.p, np, 0.0, Z + (long long)(k + 1) * Leq * np,
+                         np);
+                }
+            });
+            if (!res) {
+                PcResult P = pc_transform(c, Sp, Kp, np, thr);
+                acc.nnew[(plus ? 3 : 5) + 10 * s] = P.nnew;
+                // s(ab,mu) = sum_{abp} 0.5 Sf[abp, ab] C[abp, mu]
+                T smp = matmul(c, Sp, true, P.C, false);
+                axpby(c, np * np, 0.5, smp.p, 0.0, nullptr, smp.p);
+                T R = matmul(c, V, false, smp, false);
+                T Rj = stack_others(Leq, np, [&](int j, double *out) {
+                    T Xr = xmet(j);
+                    T sj = matmul(c, Xr, false, P.C, false);
+                    gemm(c, false, false, Leq, np, np, 1.0, V.p, np, sj.p, np, 0.0, out, np);
+                });
+                pc_accum(e2, psi2, pc_finish(R, nullptr, Rj, nullptr, P.w, pb, np, 0));
+            }
         }
         pc_store(plus ? 3 : 4, e2, psi2, false);
     }
@@ -1281,37 +1335,16 @@ class Runner {
         place(K, Kga, 0, nn, -0.5);
         place(K, Kga, nn, 0, -0.5);
         place(K, Kgd, nn, nn, 1.0);
-        PcResult P = pc_transform(c, S, K, n2, thr);
-        acc.nnew[8 + 10 * s] = P.nnew;
-        // aux: s = val C_top, sp = val C_bot, spp = val2 C_bot (val = Snw as [ab,abp])
-        T Ctop = alloc(c, {(long long)nn, n2}, false), Cbot = alloc(c, {(long long)nn, n2}, false);
-        ck(cudaMemcpyAsync(Ctop.p, P.C.p, sizeof(double) * nn * n2, cudaMemcpyDeviceToDevice, c.st), "cp");
-        ck(cudaMemcpyAsync(Cbot.p, P.C.p + nn * n2, sizeof(double) * nn * n2, cudaMemcpyDeviceToDevice, c.st), "cp");
         T val = view2(copy_of(c, Snw.p, {nn, nn}), nn, nn);
         T val2 = alloc(c, {n, n, n, n}, false);  // -daa(ap,b,a,bp) at [a,b,ap,bp] + [ap==a] 2 da(b,bp)
         gather(c, D.g2.p, 0, {n, n, n, n}, {(long long)n, (long long)n * n, (long long)n * n * n, 1}, val2.p, -1.0);
         add_diag_pairs(c, val2.p, n, 0, 2, D.g1.p, false, 2.0);
         T val2m = view2(std::move(val2), nn, nn);
-        T sA = matmul(c, val, false, Ctop, false), sP = matmul(c, val, false, Cbot, false);
-        T sPP = matmul(c, val2m, false, Cbot, false);
-        // ro vectors: gba[ab] = da(b,a)
-        T gba = permuted(c, D.g1, {1, 0});
-        T gtop = alloc(c, {1, n2}, false), gbot = alloc(c, {1, n2}, false);
-        gemm(c, false, false, 1, n2, nn, 1.0, gba.p, nn, Ctop.p, n2, 0.0, gtop.p, n2);
-        gemm(c, false, false, 1, n2, nn, 1.0, gba.p, nn, Cbot.p, n2, 0.0, gbot.p, n2);
+        T gba = permuted(c, D.g1, {1, 0});  // ro vector gba[ab] = da(b,a)
         T hdev = upload(c, hv);
-        auto rim = [&](const T &s_, const T &sp_, const T &spp_, const T &gt, const T &gb, double *out) {
-            // out[L,mu] = di s + (-dj) sp + dk spp + h (2 gt - gb)
-            gemm(c, false, false, L, n2, nn, 1.0, di.p, nn, s_.p, n2, 0.0, out, n2);
-            gemm(c, false, false, L, n2, nn, -1.0, DJ.p, nn, sp_.p, n2, 1.0, out, n2);
-            gemm(c, false, false, L, n2, nn, 1.0, DK.p, nn, spp_.p, n2, 1.0, out, n2);
-            T g = alloc(c, {1, n2}, false);
-            axpby(c, n2, 2.0, gt.p, -1.0, gb.p, g.p);
-            gemm(c, false, false, L, n2, 1, 1.0, hdev.p, 1, g.p, n2, 1.0, out, n2);
-        };
-        T R = alloc(c, {L, n2}, false);
-        rim(sA, sP, sPP, gtop, gbot, R.p);
-        T Rj = stack_others(L, n2, [&](int j, double *out) {
+        // the matrices of another state j: v ~ val, v2 ~ val2, ro ~ gba
+        struct OtherMats { T v, v2, ro; };
+        auto other_mats = [&](int j) {
             auto [PD, lt] = off(j);
             T E2o = alloc(c, {n, n, n, n}, false);
             build_ee2L(c, PD->d2.p, PD->d1.p, n, E2o.p);
@@ -1326,30 +1359,93 @@ class Runner {
                        {(long long)n, (long long)n * n, (long long)n * n * n, 1}, v2.p, -1.0);
                 add_diag_pairs(c, v2.p, n, 0, 2, PD->d1.p, false, 2.0);
             }
-            T vm = view2(std::move(v), nn, nn), v2m = view2(std::move(v2), nn, nn);
-            T sj = matmul(c, vm, false, Ctop, false), spj = matmul(c, vm, false, Cbot, false);
-            T sppj = matmul(c, v2m, false, Cbot, false);
             T ro = lt ? permuted(c, PD->d1, {1, 0}) : copy_of(c, PD->d1.p, {n, n});  // daoff(b,a) / daoff(a,b)
-            T gt = alloc(c, {1, n2}, false), gb = alloc(c, {1, n2}, false);
-            gemm(c, false, false, 1, n2, nn, 1.0, ro.p, nn, Ctop.p, n2, 0.0, gt.p, n2);
-            gemm(c, false, false, 1, n2, nn, 1.0, ro.p, nn, Cbot.p, n2, 0.0, gb.p, n2);
-            rim(sj, spj, sppj, gt, gb, out);
-        });
+            return OtherMats{view2(std::move(v), nn, nn), view2(std::move(v2), nn, nn), std::move(ro)};
+        };
         std::vector<double> pb(L);
         for (long long l = 0; l < L; ++l) pb[l] = -base[l];  // deno = w + eps_r - eps_i
         std::vector<double> e2(M * M, 0.0);
         double psi2 = 0.0;
+        const int nrho = acc.rho ? 1 : 0;
+        auto store_rho = [&](const std::vector<double> &rl) {
+            for (int i = 0; i < nc; ++i)
+                for (int r = 0; r < nv; ++r) acc.rhoir[i + (size_t)nc * (r + (size_t)nv * s)] += rl[(size_t)i * nv + r];
+        };
+        PencilTridiag PT;
+        if (metric_above(c, S.p, n2, thr) && pencil_tridiag(c, K.p, S.p, n2, PT)) {
+            // every metric eigenvalue is kept: resolvents of the pencil (as in
+            // the (+-1') classes) on the numerators before the PC basis change,
+            //   z = [di A1 + 2 h g1 | -dj A1 + dk A2 - h g1]   (R = z C),
+            // and for the density the vector g = [2 da | -da] (vaux = g C)
+            acc.nnew[8 + 10 * s] = (int)n2;
+            const long long rows = (long long)M * L + nrho;
+            T Z = alloc(c, {rows, n2}, false);
+            auto zrows = [&](const T &A1, const T &A2, const double *g1, double *out) {
+                gemm(c, false, false, L, nn, nn, 1.0, di.p, nn, A1.p, nn, 0.0, out, n2);
+                gemm(c, false, false, L, nn, 1, 2.0, hdev.p, 1, g1, nn, 1.0, out, n2);
+                gemm(c, false, false, L, nn, nn, -1.0, DJ.p, nn, A1.p, nn, 0.0, out + nn, n2);
+                gemm(c, false, false, L, nn, nn, 1.0, DK.p, nn, A2.p, nn, 1.0, out + nn, n2);
+                gemm(c, false, false, L, nn, 1, -1.0, hdev.p, 1, g1, nn, 1.0, out + nn, n2);
+            };
+            zrows(val, val2m, gba.p, Z.p);
+            auto o = others();
+            for (size_t k = 0; k < o.size(); ++k) {
+                OtherMats m = other_mats(o[k]);
+                zrows(m.v, m.v2, m.ro.p, Z.p + (long long)(k + 1) * L * n2);
+            }
+            if (nrho) {
+                double *g = Z.p + (long long)M * L * n2;
+                axpby(c, nn, 2.0, D.g1.p, 0.0, nullptr, g);
+                axpby(c, nn, -1.0, D.g1.p, 0.0, nullptr, g + nn);
+            }
+            pencil_rhs(c, PT, Z.p, rows);
+            T Yt = permuted(c, Z, {1, 0});  // [n2][M L + nrho]
+            T rho = alloc(c, {L, 1}, true);
+            pc_accum(e2, psi2, resolvent_sums(PT, Yt, pb, nrho, (long long)M * L, rho.p));
+            pc_store(7, e2, psi2, true);
+            if (nrho) store_rho(download(c, rho.p, L));
+            return;
+        }
+        PcResult P = pc_transform(c, S, K, n2, thr);
+        acc.nnew[8 + 10 * s] = P.nnew;
+        // aux: s = val C_top, sp = val C_bot, spp = val2 C_bot (val = Snw as [ab,abp])
+        T Ctop = alloc(c, {(long long)nn, n2}, false), Cbot = alloc(c, {(long long)nn, n2}, false);
+        ck(cudaMemcpyAsync(Ctop.p, P.C.p, sizeof(double) * nn * n2, cudaMemcpyDeviceToDevice, c.st), "cp");
+        ck(cudaMemcpyAsync(Cbot.p, P.C.p + nn * n2, sizeof(double) * nn * n2, cudaMemcpyDeviceToDevice, c.st), "cp");
+        T sA = matmul(c, val, false, Ctop, false), sP = matmul(c, val, false, Cbot, false);
+        T sPP = matmul(c, val2m, false, Cbot, false);
+        T gtop = alloc(c, {1, n2}, false), gbot = alloc(c, {1, n2}, false);
+        gemm(c, false, false, 1, n2, nn, 1.0, gba.p, nn, Ctop.p, n2, 0.0, gtop.p, n2);
+        gemm(c, false, false, 1, n2, nn, 1.0, gba.p, nn, Cbot.p, n2, 0.0, gbot.p, n2);
+        auto rim = [&](const T &s_, const T &sp_, const T &spp_, const T &gt, const T &gb, double *out) {
+            // out[L,mu] = di s + (-dj) sp + dk spp + h (2 gt - gb)
+            gemm(c, false, false, L, n2, nn, 1.0, di.p, nn, s_.p, n2, 0.0, out, n2);
+            gemm(c, false, false, L, n2, nn, -1.0, DJ.p, nn, sp_.p, n2, 1.0, out, n2);
+            gemm(c, false, false, L, n2, nn, 1.0, DK.p, nn, spp_.p, n2, 1.0, out, n2);
+            T g = alloc(c, {1, n2}, false);
+            axpby(c, n2, 2.0, gt.p, -1.0, gb.p, g.p);
+            gemm(c, false, false, L, n2, 1, 1.0, hdev.p, 1, g.p, n2, 1.0, out, n2);
+        };
+        T R = alloc(c, {L, n2}, false);
+        rim(sA, sP, sPP, gtop, gbot, R.p);
+        T Rj = stack_others(L, n2, [&](int j, double *out) {
+            OtherMats m = other_mats(j);
+            T sj = matmul(c, m.v, false, Ctop, false), spj = matmul(c, m.v, false, Cbot, false);
+            T sppj = matmul(c, m.v2, false, Cbot, false);
+            T gt = alloc(c, {1, n2}, false), gb = alloc(c, {1, n2}, false);
+            gemm(c, false, false, 1, n2, nn, 1.0, m.ro.p, nn, Ctop.p, n2, 0.0, gt.p, n2);
+            gemm(c, false, false, 1, n2, nn, 1.0, m.ro.p, nn, Cbot.p, n2, 0.0, gb.p, n2);
+            rim(sj, spj, sppj, gt, gb, out);
+        });
         pc_accum(e2, psi2, pc_finish(R, nullptr, Rj, nullptr, P.w, pb, n2, 0));
         pc_store(7, e2, psi2, true);
-        if (acc.rho) {
+        if (nrho) {
             // e20pcont :4854-4860, :4971-4975: rhoir(i,r) -= sum_mu c_mu vaux_mu with
             // vaux_mu = sum_ab da(a,b) (2 coef(ab,mu) - coef(ab+nn,mu))
             T v = alloc(c, {1, n2}, false);
             gemm(c, false, false, 1, n2, nn, 2.0, D.g1.p, nn, Ctop.p, n2, 0.0, v.p, n2);
             gemm(c, false, false, 1, n2, nn, -1.0, D.g1.p, nn, Cbot.p, n2, 1.0, v.p, n2);
-            auto rl = rho_pc(R, v, P.w, pb, n2, 1);
-            for (int i = 0; i < nc; ++i)
-                for (int r = 0; r < nv; ++r) acc.rhoir[i + (size_t)nc * (r + (size_t)nv * s)] += rl[(size_t)i * nv + r];
+            store_rho(rho_pc(R, v, P.w, pb, n2, 1));
         }
     }
 

@@ -77,9 +77,25 @@ def upper_sym(A):
     return np.triu(A) + np.triu(A, 1).T
 
 
+# Above this order LAPACK dsyev (the reference's driver: QR iteration with
+# eigenvector accumulation) is ~30x slower than divide and conquer (105 s vs
+# 3.6 s at order 4096 on 8 cores); there the oracle calls dsyevd.
+DSYEV_MAX_ORDER = 1024
+
+
+def eigh_ref(A, lower):
+    """The reference's dsyev on the symmetric matrix A (already symmetric):
+    LAPACK dsyev up to DSYEV_MAX_ORDER, dsyevd above.  Both are backward
+    stable; on the ill-conditioned synthetic CAS(16,16) classes they are the
+    two most accurate FP64 LAPACK drivers (MRRR, scipy's default, was 10-100x
+    further from an extended-precision evaluation)."""
+    drv = "ev" if A.shape[0] <= DSYEV_MAX_ORDER else "evd"
+    return sla.eigh(A, lower=lower, driver=drv)
+
+
 def dsyev_u(A):
     """dsyev('V','U'): eigenpairs of the matrix whose upper triangle is A's."""
-    return sla.eigh(upper_sym(A), lower=False)
+    return eigh_ref(upper_sym(A), lower=False)
 
 
 def pc_transform(S, K, thr):
@@ -271,12 +287,12 @@ class _State:
         # dsyev('V','L'): the lower triangle is the one filled in the reference
         if nc:
             Fc = fock(core)
-            wc, Uc = sla.eigh(np.tril(Fc) + np.tril(Fc, -1).T, lower=True)
+            wc, Uc = eigh_ref(np.tril(Fc) + np.tril(Fc, -1).T, lower=True)
             eps[core] = wc
         else:
             Uc = np.zeros((0, 0))
         Fv = fock(virt)
-        wv, Uv = sla.eigh(np.tril(Fv) + np.tril(Fv, -1).T, lower=True)
+        wv, Uv = eigh_ref(np.tril(Fv) + np.tril(Fv, -1).T, lower=True)
         eps[virt] = wv
         self.eps = eps
         U = np.zeros((norb, norb))
