@@ -737,7 +737,10 @@ class Runner {
         if (L > 0 && n > 0) {
             const size_t smem = sizeof(double) * 6 * (size_t)n;
             if (smem > 227 * 1024) throw Error(NVPT_EINVAL, "resolvent: pencil order above the shared-memory limit");
-            ck(cudaFuncSetAttribute(k_tridiag_resolvent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+            // one value for every caller: pencils of different orders are
+            // solved concurrently on other host threads, and a per-call limit
+            // set by one of them could undercut another's launch
+            ck(cudaFuncSetAttribute(k_tridiag_resolvent, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024),
                "smem attr");
             ProfSpan sp;
             sp.begin("pencil_solve", c.st, 0);
@@ -1516,20 +1519,39 @@ class Runner {
         T Bc = copy_of(c, Bm.p, {n, n, n, n});
         permute(c, Cm.p, {n, n, n, n}, {1, 2, 3, 0}, Bc.p, 1.0, true);  // + cmat(a,ap,bp,cp)
         long long L = Lx;
+        // With PC, the order-n^3 products of the SC forms are the first terms
+        // of the PC numerators, so they are formed once: own state
+        // dp'W3 dp = diag(Vd S Vd^T) with the metric S = W3^T (the diagonal of
+        // a quadratic form does not see the transpose); another state j:
+        // Vd W3o_j is Vd S_j, S_j the transition metric of its numerators.
+        T S, Yown;
+        std::map<int, T> yoth;
+        if (pc) {
+            S = view2(permuted(c, W3, {3, 4, 5, 0, 1, 2}), n3, n3);  // [(a,b,c),(ap,bp,cp)]
+            Yown = alloc(c, {L, (long long)n3}, false);
+            gemm(c, false, false, L, n3, n3, 1.0, Vd.p, n3, S.p, n3, 0.0, Yown.p, n3);
+        }
         // dumm = h'rho h + 2 dp'W2 h + dp'W3 dp ; dumk = h'Dm h + dp'Bc h + dp'A dp
-        auto form3 = [&](const double *rho_, const double *w2, double c2, const double *w3, double *out) {
+        // (y3pre: Vd W3 or a product with the same diagonal form; y3keep: keep Vd W3)
+        auto form3 = [&](const double *rho_, const double *w2, double c2, const double *w3, double *out,
+                         const T *y3pre, T *y3keep) {
             T q = bilin(c, H, rho_, n, H);
             T y = alloc(c, {L, (long long)n}, false);
             gemm(c, false, false, L, n, n3, 1.0, Vd.p, n3, w2, n, 0.0, y.p, n);  // dp' W2
             rowdot_acc(c, y, H, q.p, c2);
-            T y3 = alloc(c, {L, (long long)n3}, false);
-            gemm(c, false, false, L, n3, n3, 1.0, Vd.p, n3, w3, n3, 0.0, y3.p, n3);
-            rowdot_acc(c, y3, Vd, q.p, 1.0);
+            if (y3pre) {
+                rowdot_acc(c, *y3pre, Vd, q.p, 1.0);
+            } else {
+                T y3 = alloc(c, {L, (long long)n3}, false);
+                gemm(c, false, false, L, n3, n3, 1.0, Vd.p, n3, w3, n3, 0.0, y3.p, n3);
+                rowdot_acc(c, y3, Vd, q.p, 1.0);
+                if (y3keep) *y3keep = std::move(y3);
+            }
             ck(cudaMemcpyAsync(out, q.p, sizeof(double) * L, cudaMemcpyDeviceToDevice, c.st), "cp");
         };
         T dumm = alloc(c, {L}, false), dumk = alloc(c, {L}, false);
-        form3(rho.p, W2.p, 2.0, W3.p, dumm.p);
-        form3(Dm.p, Bc.p, 1.0, A.p, dumk.p);
+        form3(rho.p, W2.p, 2.0, W3.p, dumm.p, pc ? &Yown : nullptr, nullptr);
+        form3(Dm.p, Bc.p, 1.0, A.p, dumk.p, nullptr, nullptr);
         T dnj = stack_others(L, 1, [&](int j, double *out) {
             auto [P, lt] = off(j);
             T E2o = alloc(c, {n, n, n, n}, false), E3o = alloc(c, {n, n, n, n, n, n}, false);
@@ -1560,7 +1582,7 @@ class Runner {
             // j<i: (cp,ap,bp,b,a,c); j>i: (c,a,b,bp,ap,cp) at [ap,bp,cp,a,b,c]
             if (lt) permute(c, e3src->p, {n, n, n, n, n, n}, {1, 2, 0, 4, 3, 5}, W3o.p);
             else permute(c, e3src->p, {n, n, n, n, n, n}, {4, 3, 5, 1, 2, 0}, W3o.p);
-            form3(ro.p, W2o.p, 1.0, W3o.p, out);
+            form3(ro.p, W2o.p, 1.0, W3o.p, out, nullptr, pc ? &yoth[j] : nullptr);
         });
         std::vector<double> base(L);
         for (long long l = 0; l < L; ++l) base[l] = minus ? -eps[nc + na + l] : eps[l];
@@ -1568,42 +1590,33 @@ class Runner {
         sc_store(minus ? 6 : 5, res);
         if (!pc) return;
         // ---- PC: metric and Koopmans matrix of order n^3 ----
-        T S = permuted(c, W3, {3, 4, 5, 0, 1, 2});  // [(a,b,c),(ap,bp,cp)]
         T K = permuted(c, A, {3, 4, 5, 0, 1, 2});
-        S = view2(std::move(S), n3, n3);
         K = view2(std::move(K), n3, n3);
         T W2t = permuted(c, W2, {3, 0, 1, 2});                 // [a, (ap,bp,cp)]
         W2t = view2(std::move(W2t), n, n3);
         // Z[l, x] = (Vd S + H W2t)[l, x]: the numerators of the reference
-        // before the change to the PC basis (R = Z C).
-        auto zm = [&](const T &S_, const T &W2_, double *out) {
-            gemm(c, false, false, L, n3, n3, 1.0, Vd.p, n3, S_.p, n3, 0.0, out, n3);
+        // before the change to the PC basis (R = Z C); Y = Vd S was formed above.
+        auto zm = [&](const T &Y, const T &W2_, double *out) {
+            ck(cudaMemcpyAsync(out, Y.p, sizeof(double) * L * n3, cudaMemcpyDeviceToDevice, c.st), "cp");
             gemm(c, false, false, L, n3, n, 1.0, H.p, n, W2_.p, n3, 1.0, out, n3);
         };
         // the same rows with the transition metric of another state j
+        // The first term Vd S_j, with S_j the transition metric [(a,b,c),(ap,bp,cp)]
+        // of eee2(c,a,b,bp,ap,cp) (j<i) / eee2(cp,ap,bp,b,a,c) (j>i) -- eee2t
+        // for (+1') -- is the product kept from the SC form of state j.
         auto other_z = [&](int j, double *out) {
             auto [PD, lt] = off(j);
-            T E2o = alloc(c, {n, n, n, n}, false), E3o = alloc(c, {n, n, n, n, n, n}, false);
+            T E2o = alloc(c, {n, n, n, n}, false);
             build_ee2L(c, PD->d2.p, PD->d1.p, n, E2o.p);
-            build_eee2L(c, PD->d3.p, PD->d2.p, PD->d1.p, n, E3o.p);
-            T W3o = alloc(c, {n, n, n, n, n, n}, false), W2o = alloc(c, {n, n, n, n}, false);
-            T E3t;
-            const T *e3src = &E3o;
-            if (!minus) {
-                E3t = alloc(c, {n, n, n, n, n, n}, false);
-                build_eee2tL(c, E3o.p, E2o.p, n, E3t.p);
-                e3src = &E3t;
-            }
-            if (lt) {  // eee2(c,a,b,bp,ap,cp); minus ee2(a,bp,ap,cp) / plus ee2tl(a,bp,ap,cp)
-                permute(c, e3src->p, {n, n, n, n, n, n}, {4, 3, 5, 1, 2, 0}, W3o.p);
+            T W2o = alloc(c, {n, n, n, n}, false);
+            if (lt) {  // minus ee2(a,bp,ap,cp) / plus ee2tl(a,bp,ap,cp)
                 if (minus) permute(c, E2o.p, {n, n, n, n}, {2, 1, 3, 0}, W2o.p);
                 else {
                     T E2b = alloc(c, {n, n, n, n}, false);
                     build_ee2tlL(c, E2o.p, PD->d1.p, n, E2b.p);
                     permute(c, E2b.p, {n, n, n, n}, {2, 1, 3, 0}, W2o.p);
                 }
-            } else {   // eee2(cp,ap,bp,b,a,c); minus ee2(cp,ap,bp,a) / plus ee2tr(cp,ap,bp,a)
-                permute(c, e3src->p, {n, n, n, n, n, n}, {1, 2, 0, 4, 3, 5}, W3o.p);
+            } else {   // minus ee2(cp,ap,bp,a) / plus ee2tr(cp,ap,bp,a)
                 if (minus) permute(c, E2o.p, {n, n, n, n}, {1, 2, 0, 3}, W2o.p);
                 else {
                     T E2a = alloc(c, {n, n, n, n}, false);
@@ -1611,11 +1624,9 @@ class Runner {
                     permute(c, E2a.p, {n, n, n, n}, {1, 2, 0, 3}, W2o.p);
                 }
             }
-            T So = permuted(c, W3o, {3, 4, 5, 0, 1, 2});
-            So = view2(std::move(So), n3, n3);
             T W2ot = permuted(c, W2o, {3, 0, 1, 2});
             W2ot = view2(std::move(W2ot), n, n3);
-            zm(So, W2ot, out);
+            zm(yoth.at(j), W2ot, out);
         };
         std::vector<double> pb(L);  // deno = w + eps_r  /  w - eps_i
         for (long long l = 0; l < L; ++l) pb[l] = -base[l];
@@ -1653,7 +1664,7 @@ class Runner {
             acc.nnew[(minus ? 7 : 6) + 10 * s] = (int)n3;
             // own state, then the others, then the nd density vectors g_d
             T Z = alloc(c, {(long long)M * L + nd, (long long)n3}, false);
-            zm(S, W2t, Z.p);
+            zm(Yown, W2t, Z.p);
             auto o = others();
             for (size_t k = 0; k < o.size(); ++k) other_z(o[k], Z.p + (long long)(k + 1) * L * n3);
             if (nd)
@@ -1672,7 +1683,7 @@ class Runner {
             // R[l, mu] = sum_x Z[l, x] C[x, mu]: the order-n3 products S C and
             // W2t C of the reference are reassociated onto the L rows.
             T Z = alloc(c, {L, (long long)n3}, false), R = alloc(c, {L, (long long)n3}, false);
-            zm(S, W2t, Z.p);
+            zm(Yown, W2t, Z.p);
             gemm(c, false, false, L, n3, n3, 1.0, Z.p, n3, P.C.p, n3, 0.0, R.p, n3);
             T Rj = stack_others(L, n3, [&](int j, double *out) {
                 other_z(j, Z.p);
