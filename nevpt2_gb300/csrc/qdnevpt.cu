@@ -736,12 +736,10 @@ class Runner {
         T a = alloc(c, {2 + 8}, true);
         if (L > 0 && n > 0) {
             const size_t smem = sizeof(double) * 6 * (size_t)n;
-            if (smem > 227 * 1024) throw Error(NVPT_EINVAL, "resolvent: pencil order above the shared-memory limit");
-            // one value for every caller: pencils of different orders are
-            // solved concurrently on other host threads, and a per-call limit
-            // set by one of them could undercut another's launch
-            ck(cudaFuncSetAttribute(k_tridiag_resolvent, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024),
-               "smem attr");
+            // one limit for every caller: pencils of different orders are
+            // solved concurrently on other host threads
+            const int lim = raise_dynamic_smem((const void *)k_tridiag_resolvent);
+            if ((long long)smem > lim) throw Error(NVPT_EINVAL, "resolvent: pencil order above the shared-memory limit");
             ProfSpan sp;
             sp.begin("pencil_solve", c.st, 0);
             k_tridiag_resolvent<<<(unsigned)L, 128, smem, c.st>>>(PT.d.p, PT.e.p, n, Yt.p, Yt.sh[1], L, M - 1, sg.p,

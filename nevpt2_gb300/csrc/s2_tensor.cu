@@ -329,6 +329,17 @@ void gram(Ctx &c, const double *X, long long Q, long long m, double *out) {
     g_launches.fetch_add(1, std::memory_order_relaxed);
 }
 
+int raise_dynamic_smem(const void *kernel) {
+    cudaFuncAttributes fa{};
+    ck(cudaFuncGetAttributes(&fa, kernel), "cudaFuncGetAttributes");
+    int dev = 0, optin = 0;
+    ck(cudaGetDevice(&dev), "cudaGetDevice");
+    ck(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "attr");
+    const int lim = optin - (int)fa.sharedSizeBytes;
+    ck(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, lim), "smem attr");
+    return lim;
+}
+
 bool metric_above(Ctx &c, const double *A, long long n, double thr) {
     if (n == 0) return true;
     double *M = nullptr, *work = nullptr;

@@ -123,6 +123,11 @@ void gram(Ctx &c, const double *X, long long Q, long long m, double *out);
 // True if every eigenvalue of the symmetric matrix (upper triangle of A) is
 // above thr: a Cholesky factorisation of A - thr I succeeds.
 bool metric_above(Ctx &c, const double *A, long long n, double thr);
+// Raise kernel's dynamic shared-memory limit to the most the current device
+// allows next to its static shared memory, and return that limit.  The value
+// is the same for every caller, so host threads launching the kernel with
+// different sizes concurrently cannot undercut one another's launches.
+int raise_dynamic_smem(const void *kernel);
 // Generalised symmetric-definite eigenproblem K v = w S v (upper triangles;
 // cusolverDnDsygvd): w ascending, V[k][i] = component i of eigenvector k,
 // eigenvectors S-orthonormal.  False if S is not positive definite.

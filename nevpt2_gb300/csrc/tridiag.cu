@@ -307,13 +307,11 @@ int sytrd_lower(Ctx &c, double *A, long long n, double *d, double *e, double *ta
     ck(cudaGetDevice(&dev), "cudaGetDevice");
     ck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "attr");
     const size_t vbytes = sizeof(double) * (size_t)n;  // v of the current column in shared memory
-    constexpr int kMaxColumnBytes = 200 * 1024;
-    if (vbytes > kMaxColumnBytes) throw Error(1, "sytrd: order too large for the shared-memory column");
     // one limit for every caller: tridiagonalisations of different orders run
-    // concurrently on other host threads, and a per-call limit set by one of
-    // them could undercut another's launch
-    ck(cudaFuncSetAttribute(k_sytrd_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxColumnBytes),
-       "smem attr");
+    // concurrently on other host threads
+    const int lim = raise_dynamic_smem((const void *)k_sytrd_panel);
+    if (vbytes > 200 * 1024 || (long long)vbytes > lim)
+        throw Error(1, "sytrd: order too large for the shared-memory column");
     ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sytrd_panel, TT, vbytes), "occupancy");
     if (per < 1) throw Error(2, "sytrd panel kernel cannot be resident");
     // 1/share of the SMs per tridiagonalisation: the pencils of a QD step
