@@ -294,6 +294,18 @@ int nvpt_profile_read(nvpt_context *ctx, const char *tag, double *ms, int64_t *l
  * No counterpart in the reference; for callers that want a tighter bound. */
 int nvpt_set_wait_limit(nvpt_context *ctx, int64_t polls);
 
+/* Route of the PC classes in nvpt_qdnevpt (no counterpart in the reference,
+ * which always diagonalises).  mode 0 (default): the order-n^3 metrics of
+ * the (+-1') classes (order >= 512) are evaluated as resolvents of the pencil
+ * K v = w S v when every metric eigenvalue is kept; the other classes follow
+ * the reference's eigenpair sequence.  mode 1: every PC class whose metric
+ * keeps all eigenvalues (the (+-2), (0') and (+-1') metrics of any order)
+ * takes the resolvent route -- closer to the exact sums on near-singular
+ * denominators, and slower: the small pencils add FP64 triangular solves on
+ * every label and grid-synchronised tridiagonalisations that compete with
+ * the large ones. */
+int nvpt_set_pc_route(nvpt_context *ctx, int mode);
+
 /* Autotuning of launch parameters (no counterpart in the reference).  With
  * on = 1, the first call that meets a new shape of a tuned kernel times
  * every candidate of its parameter with CUDA events on the call's stream

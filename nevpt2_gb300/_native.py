@@ -89,6 +89,7 @@ _SIGS = {
     "nvpt_bdmat_d": ([P] + [P] * 5 + [I64, I64, P, P, I64, P], ctypes.c_int),
     "nvpt_set_autotune": ([P, ctypes.c_int], ctypes.c_int),
     "nvpt_set_wait_limit": ([P, I64], ctypes.c_int),
+    "nvpt_set_pc_route": ([P, ctypes.c_int], ctypes.c_int),
     "nvpt_autotune_report": ([P, ctypes.c_char_p, I64], I64),
     "nvpt_h5c_write": ([ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int],
                        ctypes.c_int),
@@ -162,6 +163,11 @@ class Context:
     def autotune(self, on: bool = True) -> None:
         """nvpt_set_autotune: tune the launch parameters of new shapes."""
         self.call("nvpt_set_autotune", 1 if on else 0)
+
+    def pc_route(self, mode: int) -> None:
+        """nvpt_set_pc_route: 0 = resolvents for the order-n^3 (+-1') pencils
+        only (default), 1 = for every PC class whose metric is kept whole."""
+        self.call("nvpt_set_pc_route", int(mode))
 
     def autotune_report(self) -> dict:
         """The tuned choices (nvpt_autotune_report) as a dict."""

@@ -127,6 +127,7 @@ struct nvpt_context {
     long long launches_at_create = 0;
     IjklState ijkl;
     unsigned wait_limit = 0;  // nvpt_set_wait_limit (0 = built-in)
+    int pc_route = 0;         // nvpt_set_pc_route
 };
 
 namespace {
@@ -290,6 +291,14 @@ unsigned nvpt_context_wait_limit(const nvpt_context *ctx) { return ctx ? ctx->wa
 int nvpt_set_wait_limit(nvpt_context *ctx, int64_t polls) {
     if (!ctx || polls < 0 || polls > 0xffffffffLL) return NVPT_EINVAL;
     ctx->wait_limit = (unsigned)polls;
+    return NVPT_OK;
+}
+
+int nvpt_context_pc_route(const nvpt_context *ctx) { return ctx ? ctx->pc_route : 0; }
+
+int nvpt_set_pc_route(nvpt_context *ctx, int mode) {
+    if (!ctx || mode < 0 || mode > 1) return NVPT_EINVAL;
+    ctx->pc_route = mode;
     return NVPT_OK;
 }
 

@@ -29,6 +29,7 @@
 #include "s2_tensor.cuh"
 
 extern "C" unsigned nvpt_context_wait_limit(const nvpt_context *ctx);
+extern "C" int nvpt_context_pc_route(const nvpt_context *ctx);
 
 namespace nvpt {
 namespace s2 {
@@ -758,7 +759,7 @@ class Runner {
     bool pc_resolvent(const T &S, const T &K, long long nd, long long L, int nnew_slot,
                       const std::vector<double> &shift, std::vector<double> &e2, double &psi2,
                       const std::function<void(double *)> &fill) {
-        if (nd == 0 || L == 0) return false;
+        if (nd == 0 || L == 0 || !c.all_pc_resolvent) return false;
         PencilTridiag PT;
         if (!(metric_above(c, S.p, nd, thr) && pencil_tridiag(c, K.p, S.p, nd, PT))) return false;
         acc.nnew[nnew_slot + 10 * s] = (int)nd;
@@ -1373,7 +1374,7 @@ class Runner {
                 for (int r = 0; r < nv; ++r) acc.rhoir[i + (size_t)nc * (r + (size_t)nv * s)] += rl[(size_t)i * nv + r];
         };
         PencilTridiag PT;
-        if (metric_above(c, S.p, n2, thr) && pencil_tridiag(c, K.p, S.p, n2, PT)) {
+        if (c.all_pc_resolvent && metric_above(c, S.p, n2, thr) && pencil_tridiag(c, K.p, S.p, n2, PT)) {
             // every metric eigenvalue is kept: resolvents of the pencil (as in
             // the (+-1') classes) on the numerators before the PC basis change,
             //   z = [di A1 + 2 h g1 | -dj A1 + dk A2 - h g1]   (R = z C),
@@ -1654,7 +1655,8 @@ class Runner {
                 }
         };
         PencilTridiag PT;
-        if (n3 >= kPcCholMin && metric_above(c, S.p, n3, thr) && pencil_tridiag(c, K.p, S.p, n3, PT)) {
+        if ((n3 >= kPcCholMin || c.all_pc_resolvent) && metric_above(c, S.p, n3, thr) &&
+            pencil_tridiag(c, K.p, S.p, n3, PT)) {
             // Every metric eigenvalue is kept (nnew = n3): the PC sums over
             // the eigenpairs of K v = w S v are resolvents of the pencil,
             //   sum_mu r_mu^2 / (w_mu + s) = z^T (K + s S)^-1 z,
@@ -1795,6 +1797,7 @@ struct ClassStreams {
             x.oz_err = nullptr;
             x.sm_share = 1;
             x.wait_limit = 0;
+            x.all_pc_resolvent = false;
         }
         CtxPool::release(c, dev);
     }
@@ -1937,6 +1940,7 @@ int run_qdnevpt(nvpt_context *ctx, cudaStream_t st, const nvpt_qdnevpt_in *in, n
             // measured: 8 pencils (4 states) fastest on quarters; 2 pencils on the whole GPU each
             pc_.sm_share = pc && pencils >= 4 ? 4 : 1;
             pc_.wait_limit = nvpt_context_wait_limit(ctx);
+            pc_.all_pc_resolvent = nvpt_context_pc_route(ctx) == 1;
         }
     ck(cudaEventRecord(ps.prep, c.st), "event");  // B and h ready
     std::vector<std::unique_ptr<Runner>> SR(M);

@@ -89,6 +89,9 @@ struct Ctx {
     // Polls a device-side wait (grid barrier) makes before it gives up and
     // the call reports NVPT_ETIMEDOUT; 0 = the built-in limit.
     unsigned wait_limit = 0;
+    // Resolvents (no eigenvectors) for every PC class whose metric keeps all
+    // its eigenvalues, not only the order-n^3 pencils of the (+-1') classes.
+    bool all_pc_resolvent = false;
 };
 
 T alloc(Ctx &c, std::initializer_list<long long> shape, bool zero = true);

@@ -62,7 +62,7 @@ def solve_batched(A, b):
     return x
 
 
-def plus2_pc_energy(inp, st, s, dtype=np.longdouble, chunk=64):
+def plus2_pc_energy(inp, st, s, dtype=np.longdouble, chunk=64, lapack=False):
     """-sum y^T (K - sigma S)^-1 y over the (+2) PC labels of state s in
     ``dtype``: part (a), inactive pairs i < j on the n^2 metric (fillcm2),
     and part (b), i = j on the n(n+1)/2 metric (fillcm2p); the same operands
@@ -91,7 +91,8 @@ def plus2_pc_energy(inp, st, s, dtype=np.longdouble, chunk=64):
             dint = np.stack([x[1] for x in lab]).astype(dtype)
             y = dint @ Dx.T
             A = Kx[None, :, :] - sig[:, None, None] * Sx[None, :, :]
-            x = solve_batched(A, y)
+            x = (np.stack([sla.solve(A[k], y[k]) for k in range(len(lab))]) if lapack
+                 else solve_batched(A, y))
             tot += np.sum(y * x)
         return -tot
 
@@ -115,6 +116,33 @@ def plus2_pc_energy(inp, st, s, dtype=np.longdouble, chunk=64):
         lb.append((2 * np.longdouble(eps[i]), np.where(iu == ju, tr[ju, iu], 2.0 * tr[ju, iu])))
     eb = part(q.upper_sym(Sp), q.upper_sym(Kp), 0.5 * Sp, lb)
     return ea + eb
+
+
+def sensitivity(inp, st, s, draws=2, seed=1):
+    """Largest change of the FP64 resolvent value of the (+2) class over
+    ``draws`` random perturbations: one relative rounding (2^-52 xi, xi ~
+    N(0,1)) of every orbital energy / 2-EA element / 2-HRDM element, and
+    2^-52 max|2-EA| xi added to every 2-EA element."""
+    rng = np.random.default_rng(seed)
+    e0 = plus2_pc_energy(inp, st, s, np.float64, lapack=True)
+    hr, ea, eps = inp.hrdm[s], inp.eako2[s], st.eps
+    u = 2.0 ** -52
+    cases = {
+        "eps_one_rounding": lambda: (hr, ea, eps * (1 + u * rng.standard_normal(eps.shape))),
+        "eako2_one_rounding": lambda: (hr, ea * (1 + u * rng.standard_normal(ea.shape)), eps),
+        "hrdm_one_rounding": lambda: (hr * (1 + u * rng.standard_normal(hr.shape)), ea, eps),
+        "eako2_one_rounding_of_max": lambda: (hr, ea + u * np.abs(ea).max() * rng.standard_normal(ea.shape), eps),
+    }
+    out = {}
+    for name, make in cases.items():
+        worst = 0.0
+        for _ in range(draws):
+            h2, e2, ep = make()
+            inp.hrdm[s], inp.eako2[s], st.eps = h2, e2, ep
+            worst = max(worst, abs(plus2_pc_energy(inp, st, s, np.float64, lapack=True) - e0))
+        out[name] = worst
+    inp.hrdm[s], inp.eako2[s], st.eps = hr, ea, eps
+    return out
 
 
 def stage2_inputs(p):
@@ -143,6 +171,9 @@ def main(argv=None):
     ap.add_argument("--states", type=int, nargs="*")
     ap.add_argument("--gpu", help="a bench JSON line whose energies.per_class_pc holds the GPU's values")
     ap.add_argument("--inputs", help="npz from bench.py --parity --parity-dump: the GPU's inputs and energies")
+    ap.add_argument("--sensitivity", action="store_true",
+                    help="also the change of the FP64 resolvent value under one relative rounding of the orbital "
+                         "energies, of the 2-EA / 2-HRDM elements, and one rounding of the largest 2-EA element")
     a = ap.parse_args(argv)
     t0 = time.perf_counter()
     p = synth.config_problem(a.config, with_ro4=False, with_trdm=False)
@@ -188,6 +219,8 @@ def main(argv=None):
         if gpu is not None:
             row["gpu"] = gpu[s][3]
             row["gpu_err"] = float(np.longdouble(gpu[s][3]) - ext)
+        if a.sensitivity:
+            row["sensitivity_eh"] = sensitivity(inp, st, s)
         row["longdouble_eps"] = float(np.finfo(np.longdouble).eps)
         row["extended_s"] = round(time.perf_counter() - t1, 1)
         print(json.dumps(row), flush=True)

@@ -107,3 +107,27 @@ def test_pm1p_resolvent_route_against_oracle(gpu_ctx, metat):
         for slot, key in ((6, (5, s)), (7, (6, s))):
             assert got.nnew[slot, s] == ref.nnew[key]
         assert got.nnew[6, s] == 512 and got.nnew[7, s] == 512  # the resolvent route was taken
+
+
+# nvpt_set_pc_route(ctx, 1): every PC class whose metric keeps all its
+# eigenvalues -- here the (+-2) metrics of orders n^2 and n(n+1)/2, the (0')
+# metric of order 2n^2 and the (+-1') metrics of order n^3 < 512 -- takes the
+# resolvent route instead of the eigenpair sequence.
+def test_resolvent_route_for_every_full_metric(gpu_ctx):
+    from nevpt2_gb300.koopro import context
+    n = 6
+    p = synth.make_problem(n, 6, 3, 5, metat=2, seed=10, with_trdm=True)
+    ctx = context()
+    ctx.pc_route(1)
+    try:
+        ref, got = run_both(p)
+    finally:
+        ctx.pc_route(0)
+    compare(ref, got)
+    full = {2: n * n, 3: n * (n + 1) // 2, 4: n * n, 5: n * (n + 1) // 2, 6: n ** 3, 7: n ** 3, 8: 2 * n * n}
+    keys = {2: (3, "a"), 3: (3, "b"), 4: (4, "a"), 5: (4, "b"), 6: (5,), 7: (6,), 8: (7,)}
+    for s in range(2):
+        for slot, order in full.items():
+            k = keys[slot]
+            rk = (k[0], s, k[1]) if len(k) == 2 else (k[0], s)
+            assert got.nnew[slot, s] == ref.nnew[rk] == order, (slot, s)
