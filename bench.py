@@ -545,6 +545,23 @@ def run_ours(args):
 
     s2_breakdown = stage2_breakdown()
 
+    # device time of stage 1 and of stage 2 alone (one step each, L2 flushed)
+    def stage_times():
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            ev[0].record(stream)
+            st.run(stream)
+            ev[1].record(stream)
+            flush.zero_()
+            ev[2].record(stream)
+            st.stage2(stream)
+            ev[3].record(stream)
+        torch.cuda.synchronize(dev)
+        return {"stage1_ms": round(ev[0].elapsed_time(ev[1]), 1), "stage2_ms": round(ev[2].elapsed_time(ev[3]), 1)}
+
+    stages = stage_times()
+
     # ---------------- split precision (Ozaki digits on tcgen05) ----------------
     set_mode(koopro.SPLIT)
     with torch.cuda.stream(stream):
@@ -554,6 +571,8 @@ def run_ours(args):
     clocks_sp.start()
     ms_sp, times_sp, e_sp = timed_steps(args.steps)
     clk_sp = clocks_sp.stop()
+    stages_sp = stage_times()
+    s2_breakdown_sp = stage2_breakdown()
     ctx.call("nvpt_set_profiling", 1)
     bamat_sp_ms = bamat_alone()
     oz_ms, oz_n, oz_bytes = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
@@ -701,6 +720,7 @@ def run_ours(args):
                           "peak_source": "MEASURED_PEAKS.json bf16_tflops (of measured, burst)",
                           "fp64_equivalent_tflops": (ow_tf / 64) if ow_tf else None,
                           "kernel_ms": (ow_ms.value / ow_n.value) if ow_n.value else None},
+                      "stages": stages_sp, "stage2_ms_per_piece": s2_breakdown_sp,
                       "clocks": clk_sp, "step_ms_all": times_sp},
             "roofline_bro3": {"kernel": "bro3 (k_bro3_case_a + k_bro3_combine)", "bound": "hbm", "achieved": bro3_gbs,
                               "peak": hbm_peak, "unit": "GB/s", "frac": bro3_gbs / hbm_peak, "traffic": None,
@@ -709,6 +729,7 @@ def run_ours(args):
                                                "ord8 enumeration, + n^6 outputs) per state",
                               "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
             "autotune": ctx.autotune_report(),
+            "stages": stages,
             "stage2_ms_per_piece": s2_breakdown,
             "energies": energy_summary(energies),
             "clocks": clk, "cpu_baseline": cb, "step_ms_all": times}
