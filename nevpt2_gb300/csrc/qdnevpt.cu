@@ -172,10 +172,11 @@ __global__ void k_pc_finish(const double *R, const double *Rp, const double *Rj,
 // With nd > 0 the kernel also forms rho[l nd + k] = -x . Y[:, dcol0 + k] for
 // k < nd: the first-order density of the label against nd extra right-hand
 // sides transformed with the labels' (sum_mu r_mu v_mu,k / (w_mu + sig) =
-// z^T (K + sig S)^-1 g_k with v = C^T g).
+// z^T (K + sig S)^-1 g_k with v = C^T g).  xout, when given, receives the
+// solution x of each label, row-major [n][L].
 __global__ void k_tridiag_resolvent(const double *d, const double *e, long long n, const double *Y, long long ncol,
                                     long long L, int nother, const double *sig, double *acc, int nd,
-                                    long long dcol0, double *rho) {
+                                    long long dcol0, double *rho, double *xout) {
     extern __shared__ double sm[];
     double *sd = sm, *se = sm + n, *wb = sm + 2 * n, *wc = sm + 3 * n, *wd = sm + 4 * n, *wy = sm + 5 * n;
     const long long l = blockIdx.x;
@@ -220,6 +221,8 @@ __global__ void k_tridiag_resolvent(const double *d, const double *e, long long 
         }
     }
     __syncthreads();
+    if (xout)
+        for (long long i = threadIdx.x; i < n; i += blockDim.x) xout[i * L + l] = wy[i];
     double en = 0.0, ps = 0.0;
     double offs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (long long i = threadIdx.x; i < n; i += blockDim.x) {
@@ -249,6 +252,19 @@ __global__ void k_rho_pc(const double *R, const double *V, const double *w, cons
     double acc = 0.0;
     for (long long mu = 0; mu < nmu; ++mu) acc -= R[l * nmu + mu] * V[(long long)k * nmu + mu] / (w[mu] + base[l]);
     rho[t] = acc;
+}
+
+// The QD cross terms of the resolvent route in the original basis:
+// acc[2 + k] -= sum_{l,i} Zo[(k L + l) n + i] X[l n + i] for the other states
+// k < nother (blockIdx.y), X the labels' solutions (K + sig_l S)^-1 z_l.
+__global__ void k_cross_dots(const double *Zo, const double *X, long long L, long long n, double *acc) {
+    const int k = blockIdx.y;
+    const long long tot = L * n;
+    const double *z = Zo + (long long)k * tot;
+    double s = 0.0;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += (long long)gridDim.x * blockDim.x)
+        s += z[t] * X[t];
+    block_add(-s, acc + 2 + k);
 }
 
 // v0 (class 0): labels (ii <= ij) x (r <= s); G[i,r,j,s] = (i r | j s) wait: G = Rcv^T Rcv
@@ -537,6 +553,116 @@ struct Accum {  // host mirror of the reference's energy holders
     }
 };
 
+// Non-blocking streams, each with its own cuBLAS/cuSOLVER handles, kept for
+// the life of the process (one pool per device) and lent to the concurrent
+// state / class tasks of a call; events order them against the caller's
+// stream.
+class CtxPool {
+  public:
+    static std::vector<Ctx> acquire(size_t n, int dev) {
+        CtxPool &p = get();
+        std::lock_guard<std::mutex> g(p.mu_);
+        std::vector<Ctx> out;
+        auto &free = p.free_[dev];
+        while (out.size() < n && !free.empty()) {
+            out.push_back(free.back());
+            free.pop_back();
+        }
+        while (out.size() < n) {
+            Ctx c{nullptr, nullptr, nullptr};
+            ck(cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking), "cudaStreamCreate");
+            ck(cublasCreate(&c.blas), "cublasCreate");
+            ck(cublasSetStream(c.blas, c.st), "cublasSetStream");
+            ck(cusolverDnCreate(&c.sol), "cusolverDnCreate");
+            ck(cusolverDnSetStream(c.sol, c.st), "cusolverDnSetStream");
+            out.push_back(c);
+        }
+        return out;
+    }
+    static void release(std::vector<Ctx> &v, int dev) {
+        CtxPool &p = get();
+        std::lock_guard<std::mutex> g(p.mu_);
+        for (auto &c : v) p.free_[dev].push_back(c);
+        v.clear();
+    }
+
+  private:
+    static CtxPool &get() {
+        static CtxPool pool;
+        return pool;
+    }
+    std::mutex mu_;
+    std::map<int, std::vector<Ctx>> free_;
+};
+
+// The reduction of one pencil K v = w S v on a helper stream and host thread:
+// the Cholesky check of the metric, its factorisation, the reduction to
+// standard form and the tridiagonalisation need only S and K, so they overlap
+// the caller's work on its own stream.  join() waits for them, orders the
+// caller's stream after the helper's and hands the pencil's buffers to the
+// caller's stream (where they are used and freed from then on).
+class PencilFork {
+  public:
+    PencilFork(Ctx &caller, const T &S, const T &K, long long n, double thr, PencilTridiag &pt) : c_(caller), pt_(pt) {
+        ck(cudaGetDevice(&dev_), "cudaGetDevice");
+        aux_ = CtxPool::acquire(1, dev_);
+        Ctx &a = aux_[0];
+        a.split = c_.split;
+        a.oz_err = c_.oz_err;
+        a.sm_share = c_.sm_share;
+        a.wait_limit = c_.wait_limit;
+        a.all_pc_resolvent = c_.all_pc_resolvent;
+        ck(cudaEventCreateWithFlags(&ready_, cudaEventDisableTiming), "cudaEventCreate");
+        ck(cudaEventCreateWithFlags(&done_, cudaEventDisableTiming), "cudaEventCreate");
+        ck(cudaEventRecord(ready_, c_.st), "cudaEventRecord");
+        ck(cudaStreamWaitEvent(a.st, ready_, 0), "cudaStreamWaitEvent");
+        const double *Sp = S.p, *Kp = K.p;
+        th_ = std::thread([this, Sp, Kp, n, thr]() {
+            try {
+                ck(cudaSetDevice(dev_), "cudaSetDevice");
+                ok_ = metric_above(aux_[0], Sp, n, thr) && pencil_tridiag(aux_[0], Kp, Sp, n, pt_);
+            } catch (...) {
+                err_ = std::current_exception();
+            }
+        });
+    }
+    PencilFork(const PencilFork &) = delete;
+    PencilFork &operator=(const PencilFork &) = delete;
+    // true when the metric kept every eigenvalue and the pencil is reduced
+    bool join() {
+        finish();
+        if (err_) std::rethrow_exception(err_);
+        return ok_;
+    }
+    ~PencilFork() { finish(); }
+
+  private:
+    void finish() {
+        if (th_.joinable()) th_.join();
+        if (aux_.empty()) return;
+        Ctx &a = aux_[0];
+        cudaEventRecord(done_, a.st);
+        cudaStreamWaitEvent(c_.st, done_, 0);
+        for (T *t : {&pt_.U, &pt_.A, &pt_.d, &pt_.e, &pt_.tau}) t->st = c_.st;
+        a.split = false;
+        a.oz_err = nullptr;
+        a.sm_share = 1;
+        a.wait_limit = 0;
+        a.all_pc_resolvent = false;
+        CtxPool::release(aux_, dev_);
+        cudaEventDestroy(ready_);
+        cudaEventDestroy(done_);
+    }
+    Ctx &c_;
+    PencilTridiag &pt_;
+    int dev_ = 0;
+    std::vector<Ctx> aux_;
+    cudaEvent_t ready_ = nullptr, done_ = nullptr;
+    std::thread th_;
+    std::exception_ptr err_;
+    bool ok_ = false;
+};
+
 class Runner {
   public:
     Ctx &c;
@@ -731,7 +857,8 @@ class Runner {
     // PC sums from the tridiagonal form of a pencil: Yt row-major [n][M L]
     // (column k L + l: state block k of label l), shifts per label.
     std::vector<double> resolvent_sums(const PencilTridiag &PT, const T &Yt, const std::vector<double> &shift,
-                                       int nd = 0, long long dcol0 = 0, double *rho = nullptr) {
+                                       int nd = 0, long long dcol0 = 0, double *rho = nullptr, int nother = -1,
+                                       double *xout = nullptr) {
         const long long L = (long long)shift.size(), n = PT.n;
         T sg = upload(c, shift);
         T a = alloc(c, {2 + 8}, true);
@@ -743,8 +870,9 @@ class Runner {
             if ((long long)smem > lim) throw Error(NVPT_EINVAL, "resolvent: pencil order above the shared-memory limit");
             ProfSpan sp;
             sp.begin("pencil_solve", c.st, 0);
-            k_tridiag_resolvent<<<(unsigned)L, 128, smem, c.st>>>(PT.d.p, PT.e.p, n, Yt.p, Yt.sh[1], L, M - 1, sg.p,
-                                                                   a.p, nd, dcol0, rho);
+            k_tridiag_resolvent<<<(unsigned)L, 128, smem, c.st>>>(PT.d.p, PT.e.p, n, Yt.p, Yt.sh[1], L,
+                                                                   nother < 0 ? M - 1 : nother, sg.p, a.p, nd, dcol0,
+                                                                   rho, xout);
             sp.end();
             LAUNCHED();
         }
@@ -1523,10 +1651,15 @@ class Runner {
         // dp'W3 dp = diag(Vd S Vd^T) with the metric S = W3^T (the diagonal of
         // a quadratic form does not see the transpose); another state j:
         // Vd W3o_j is Vd S_j, S_j the transition metric of its numerators.
-        T S, Yown;
+        T S, K, Yown;
         std::map<int, T> yoth;
+        PencilTridiag PT;
+        std::unique_ptr<PencilFork> fork;
         if (pc) {
             S = view2(permuted(c, W3, {3, 4, 5, 0, 1, 2}), n3, n3);  // [(a,b,c),(ap,bp,cp)]
+            K = view2(permuted(c, A, {3, 4, 5, 0, 1, 2}), n3, n3);
+            // the pencil's reduction overlaps the SC work below
+            if (n3 >= kPcCholMin || c.all_pc_resolvent) fork.reset(new PencilFork(c, S, K, n3, thr, PT));
             Yown = alloc(c, {L, (long long)n3}, false);
             gemm(c, false, false, L, n3, n3, 1.0, Vd.p, n3, S.p, n3, 0.0, Yown.p, n3);
         }
@@ -1588,9 +1721,7 @@ class Runner {
         auto res = sc_finish(dumm, dumk, base, dnj, 0);
         sc_store(minus ? 6 : 5, res);
         if (!pc) return;
-        // ---- PC: metric and Koopmans matrix of order n^3 ----
-        T K = permuted(c, A, {3, 4, 5, 0, 1, 2});
-        K = view2(std::move(K), n3, n3);
+        // ---- PC: metric S and Koopmans matrix K of order n^3 (formed above) ----
         T W2t = permuted(c, W2, {3, 0, 1, 2});                 // [a, (ap,bp,cp)]
         W2t = view2(std::move(W2t), n, n3);
         // Z[l, x] = (Vd S + H W2t)[l, x]: the numerators of the reference
@@ -1654,14 +1785,46 @@ class Runner {
                     else acc.rhoid[l + (size_t)nc * (d + (size_t)na * s)] += v;
                 }
         };
-        PencilTridiag PT;
-        if ((n3 >= kPcCholMin || c.all_pc_resolvent) && metric_above(c, S.p, n3, thr) &&
-            pencil_tridiag(c, K.p, S.p, n3, PT)) {
+        if (fork && fork->join()) {
             // Every metric eigenvalue is kept (nnew = n3): the PC sums over
             // the eigenpairs of K v = w S v are resolvents of the pencil,
             //   sum_mu r_mu^2 / (w_mu + s) = z^T (K + s S)^-1 z,
             // evaluated in the pencil's tridiagonal form (no eigenvectors).
             acc.nnew[(minus ? 7 : 6) + 10 * s] = (int)n3;
+            // The QD cross terms and the densities need z_j^T x and g_d^T x
+            // with x = (K + s S)^-1 z.  Mapping every z_j and g_d into the
+            // tridiagonal basis costs M L + nd vector transforms; mapping the L
+            // solutions back (x = U^-1 Q x~) and taking the dots in the original
+            // basis costs 2 L.  The cheaper of the two is used.
+            if (2 * L < (long long)M * L + nd) {
+                T Zo = alloc(c, {L, (long long)n3}, false);
+                zm(Yown, W2t, Zo.p);
+                auto o = others();
+                T Zx = alloc(c, {(long long)std::max<size_t>(o.size(), 1) * L, (long long)n3}, false);
+                for (size_t k = 0; k < o.size(); ++k) other_z(o[k], Zx.p + (long long)k * L * n3);
+                pencil_rhs(c, PT, Zo.p, L);
+                T Yt = permuted(c, Zo, {1, 0});  // [n3][L]
+                T Xt = alloc(c, {(long long)n3, L}, false);
+                std::vector<double> r = resolvent_sums(PT, Yt, pb, 0, 0, nullptr, 0, Xt.p);
+                T X = permuted(c, Xt, {1, 0});   // [L][n3]: the columns of a column-major [n3, L]
+                pencil_back(c, PT, X.p, L);      // x = U^-1 Q x~
+                if (!o.empty()) {
+                    T a = alloc(c, {2 + 8}, true);
+                    k_cross_dots<<<dim3((unsigned)std::min<long long>(nblk(L * n3), 1024), (unsigned)o.size()), TPB,
+                                   0, c.st>>>(Zx.p, X.p, L, n3, a.p);
+                    LAUNCHED();
+                    auto cr = download(c, a.p, 2 + 8);
+                    for (size_t k = 0; k < o.size(); ++k) r[2 + k] += cr[2 + k];
+                }
+                pc_accum(e2, psi2, r);
+                if (nd) {  // rho[l, d] = -g_d . x_l
+                    T rho = alloc(c, {L, (long long)nd}, false);
+                    gemm(c, false, true, L, nd, n3, -1.0, X.p, n3, Ed.p, n3, 0.0, rho.p, nd);
+                    store_rho(download(c, rho.p, L * nd));
+                }
+                pc_store(minus ? 6 : 5, e2, psi2, true);
+                return;
+            }
             // own state, then the others, then the nd density vectors g_d
             T Z = alloc(c, {(long long)M * L + nd, (long long)n3}, false);
             zm(Yown, W2t, Z.p);
@@ -1732,48 +1895,6 @@ T fortran_slice(Ctx &c, const T &F, long long P, long long slot, int n, int k) {
     gather(c, F.p, slot, shape, stride, out.p);
     return out;
 }
-
-// Non-blocking streams, each with its own cuBLAS/cuSOLVER handles, kept for
-// the life of the process (one pool per device) and lent to the concurrent
-// state / class tasks of a call; events order them against the caller's
-// stream.
-class CtxPool {
-  public:
-    static std::vector<Ctx> acquire(size_t n, int dev) {
-        CtxPool &p = get();
-        std::lock_guard<std::mutex> g(p.mu_);
-        std::vector<Ctx> out;
-        auto &free = p.free_[dev];
-        while (out.size() < n && !free.empty()) {
-            out.push_back(free.back());
-            free.pop_back();
-        }
-        while (out.size() < n) {
-            Ctx c{nullptr, nullptr, nullptr};
-            ck(cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking), "cudaStreamCreate");
-            ck(cublasCreate(&c.blas), "cublasCreate");
-            ck(cublasSetStream(c.blas, c.st), "cublasSetStream");
-            ck(cusolverDnCreate(&c.sol), "cusolverDnCreate");
-            ck(cusolverDnSetStream(c.sol, c.st), "cusolverDnSetStream");
-            out.push_back(c);
-        }
-        return out;
-    }
-    static void release(std::vector<Ctx> &v, int dev) {
-        CtxPool &p = get();
-        std::lock_guard<std::mutex> g(p.mu_);
-        for (auto &c : v) p.free_[dev].push_back(c);
-        v.clear();
-    }
-
-  private:
-    static CtxPool &get() {
-        static CtxPool pool;
-        return pool;
-    }
-    std::mutex mu_;
-    std::map<int, std::vector<Ctx>> free_;
-};
 
 struct ClassStreams {
     int dev = 0;

@@ -518,6 +518,28 @@ void pencil_rhs(Ctx &c, const PencilTridiag &P, double *Y, long long m) {
     if (st != 0) throw Error(2, "ormtr failed, info=" + std::to_string(st));
 }
 
+void pencil_back(Ctx &c, const PencilTridiag &P, double *X, long long m) {
+    if (P.n == 0 || m == 0) return;
+    const int N = (int)P.n, Mc = (int)m;
+    const double one = 1.0;
+    ProfSpan sp;
+    sp.begin("pencil_rhs", c.st, 0);
+    int lw = 0;
+    ck(cusolverDnDormtr_bufferSize(c.sol, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, N, Mc, P.A.p, N,
+                                   P.tau.p, X, N, &lw),
+       "ormtr_bufferSize");
+    SolverWork sw(c, lw);
+    ck(cusolverDnDormtr(c.sol, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, N, Mc, P.A.p, N, P.tau.p, X, N,
+                        sw.w, lw, sw.info),
+       "ormtr");
+    ck(cublasDtrsm(c.blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, N, Mc, &one,
+                   P.U.p, N, X, N),
+       "trsm");
+    sp.end();
+    const int st = sw.status();
+    if (st != 0) throw Error(2, "ormtr failed, info=" + std::to_string(st));
+}
+
 void build_ee2L(Ctx &c, const double *taa, const double *dal, int n, double *out) {
     long long N = (long long)n * n * n * n;
     k_ee2L<<<nblk(N), TPB, 0, c.st>>>(taa, dal, n, out);

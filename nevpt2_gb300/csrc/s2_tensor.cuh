@@ -161,6 +161,9 @@ int sytrd_lower(Ctx &c, double *A, long long n, double *d, double *e, double *ta
 // Y <- Q^T U^-T Y for Y column-major [n, m] (= row-major [m, n]): each row
 // z of the row-major view becomes y with z^T (K + s S)^-1 z = y^T (T + s)^-1 y.
 void pencil_rhs(Ctx &c, const PencilTridiag &P, double *Y, long long m);
+// The inverse map of m vectors of the tridiagonal basis (columns of a
+// column-major [n, m] X, in place): X <- U^-1 Q X.
+void pencil_back(Ctx &c, const PencilTridiag &P, double *X, long long m);
 
 // Accessor builders (C-ordered n-index tensors of one state or pair).
 void build_ee2L(Ctx &c, const double *taa, const double *dal, int n, double *out);

@@ -97,7 +97,9 @@ def test_frozen_core_and_no_pc(gpu_ctx):
 # resolvent route (Cholesky, reduction to standard form, device tridiagonalisation,
 # pivoted tridiagonal solves) whenever every metric eigenvalue is kept; the oracle
 # runs the reference's pseudo-inverse and eigenvector sequence.
-@pytest.mark.parametrize("metat", [1, 2])
+# With three states the QD cross terms are taken in the original basis (the L
+# solutions mapped back, 2L vector transforms instead of 3L).
+@pytest.mark.parametrize("metat", [1, 2, 3])
 def test_pm1p_resolvent_route_against_oracle(gpu_ctx, metat):
     p = synth.make_problem(8, 8, 4, 12, metat=metat, ndet=None if metat == 1 else 2000, seed=70 + metat,
                            with_trdm=metat > 1)
