@@ -40,7 +40,11 @@ extern "C" {
 
 typedef struct nvpt_context nvpt_context;
 
-/* Context life cycle.  `device` is the CUDA ordinal. */
+/* Context life cycle.  `device` is the CUDA ordinal.  The library's scratch
+ * is stream-ordered (cudaMallocAsync on the device's default memory pool);
+ * nvpt_create sets that pool's release threshold so that freed scratch stays
+ * in the pool between calls instead of returning to the driver at every
+ * synchronisation (cudaMemPoolTrimTo gives it back). */
 int nvpt_create(nvpt_context **ctx, int device);
 int nvpt_destroy(nvpt_context *ctx);
 int nvpt_synchronize(nvpt_context *ctx);

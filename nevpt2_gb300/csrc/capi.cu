@@ -244,6 +244,17 @@ int nvpt_create(nvpt_context **out, int device) {
         delete ctx;
         return NVPT_ECUDA;
     }
+    // The library's scratch comes from the device's default stream-ordered
+    // pool.  Its default release threshold (0) hands every freed byte back to
+    // the driver at each synchronisation, so the many allocate / synchronise /
+    // free cycles of a call (solver info words, eigenvalue read-backs) remap
+    // GBs of device memory again and again.  Keep freed memory in the pool;
+    // cudaMemPoolTrimTo returns it when the caller wants it back.
+    cudaMemPool_t pool = nullptr;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess && pool) {
+        unsigned long long keep = ~0ull;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
     ctx->launches_at_create = g_launches.load();
     *out = ctx;
     return NVPT_OK;
