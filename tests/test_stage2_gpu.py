@@ -133,3 +133,44 @@ def test_resolvent_route_for_every_full_metric(gpu_ctx):
             k = keys[slot]
             rk = (k[0], s, k[1]) if len(k) == 2 else (k[0], s)
             assert got.nnew[slot, s] == ref.nnew[rk] == order, (slot, s)
+
+
+# The (+-1') pencil reduction runs on a helper stream while the SC products
+# run; with a threshold that drops metric eigenvalues (0.3 here: ~40% of the
+# 512) its metric check fails and the task falls back to the eigenpair
+# sequence after joining it.
+def test_pm1p_metric_with_dropped_eigenvalues_after_the_fork(gpu_ctx):
+    p = synth.make_problem(8, 8, 4, 12, metat=2, ndet=2000, seed=72, with_trdm=True)
+    ref, got = run_both(p, thr=0.3, mask=0x60)
+    compare(ref, got, [5, 6])
+    for s in range(2):
+        for slot, key in ((6, (5, s)), (7, (6, s))):
+            assert got.nnew[slot, s] == ref.nnew[key] < 512
+
+
+# A grid-barrier wait of the pencil tridiagonalisation (on the helper stream
+# and thread of its class task) that runs out of polls surfaces as
+# NVPT_ETIMEDOUT from nvpt_qdnevpt, and the next call on the context is right.
+def test_pencil_timeout_inside_qdnevpt_reports_and_recovers(gpu_ctx):
+    from nevpt2_gb300._native import NvptError
+    from nevpt2_gb300.koopro import context
+    p = synth.make_problem(8, 8, 4, 12, metat=1, seed=71)
+    o = {KOOP.get(k, k): v for k, v in orc.stage1(p).items()}
+    o["1-RDM"], o["2-RDM"], o["3-RDM"] = p.dal, p.taa, p.daaa
+    ctx = context()
+    ctx.call("nvpt_set_wait_limit", 1)
+    statuses = []
+    try:
+        for _ in range(3):
+            try:
+                gq.qdnevpt(p, o, class_mask=0x60)
+                statuses.append(0)
+            except NvptError as err:
+                statuses.append(err.status)
+                if err.status == 5:
+                    break
+    finally:
+        ctx.call("nvpt_set_wait_limit", 0)
+    assert statuses[-1] == 5, statuses
+    ref, got = run_both(p, mask=0x60)
+    compare(ref, got, [5, 6])
