@@ -612,10 +612,15 @@ class PencilFork {
         a.sm_share = c_.sm_share;
         a.wait_limit = c_.wait_limit;
         a.all_pc_resolvent = c_.all_pc_resolvent;
-        ck(cudaEventCreateWithFlags(&ready_, cudaEventDisableTiming), "cudaEventCreate");
-        ck(cudaEventCreateWithFlags(&done_, cudaEventDisableTiming), "cudaEventCreate");
-        ck(cudaEventRecord(ready_, c_.st), "cudaEventRecord");
-        ck(cudaStreamWaitEvent(a.st, ready_, 0), "cudaStreamWaitEvent");
+        try {
+            ck(cudaEventCreateWithFlags(&ready_, cudaEventDisableTiming), "cudaEventCreate");
+            ck(cudaEventCreateWithFlags(&done_, cudaEventDisableTiming), "cudaEventCreate");
+            ck(cudaEventRecord(ready_, c_.st), "cudaEventRecord");
+            ck(cudaStreamWaitEvent(a.st, ready_, 0), "cudaStreamWaitEvent");
+        } catch (...) {  // no thread yet: hand the helper context back before failing
+            finish();
+            throw;
+        }
         const double *Sp = S.p, *Kp = K.p;
         th_ = std::thread([this, Sp, Kp, n, thr]() {
             try {
@@ -641,8 +646,12 @@ class PencilFork {
         if (th_.joinable()) th_.join();
         if (aux_.empty()) return;
         Ctx &a = aux_[0];
-        cudaEventRecord(done_, a.st);
-        cudaStreamWaitEvent(c_.st, done_, 0);
+        if (done_) {
+            cudaEventRecord(done_, a.st);
+            cudaStreamWaitEvent(c_.st, done_, 0);
+        } else {
+            cudaStreamSynchronize(a.st);
+        }
         for (T *t : {&pt_.U, &pt_.A, &pt_.d, &pt_.e, &pt_.tau}) t->st = c_.st;
         a.split = false;
         a.oz_err = nullptr;
@@ -650,8 +659,9 @@ class PencilFork {
         a.wait_limit = 0;
         a.all_pc_resolvent = false;
         CtxPool::release(aux_, dev_);
-        cudaEventDestroy(ready_);
-        cudaEventDestroy(done_);
+        if (ready_) cudaEventDestroy(ready_);
+        if (done_) cudaEventDestroy(done_);
+        ready_ = done_ = nullptr;
     }
     Ctx &c_;
     PencilTridiag &pt_;
