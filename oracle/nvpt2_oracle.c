@@ -1,6 +1,6 @@
 /*
  * CPU oracle for the Koopmans-matrix stage of NEVPT2 (stage 1 of the reference,
- * `koopro4QD.x`).  TEST INFRASTRUCTURE ONLY: this file is the checker that the
+ * `koopro4QD.x`).  TEST INFRASTRUCTURE ONLY: this file is the oracle that the
  * CUDA library is compared against, and the scalar CPU baseline that the bench
  * reports beside the GPU numbers.  Nothing in the product links it.
  *

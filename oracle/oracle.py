@@ -1,6 +1,6 @@
 """ctypes front end of the CPU oracle (oracle/nvpt2_oracle.c).
 
-TEST INFRASTRUCTURE ONLY: the checker the CUDA library is compared against,
+TEST INFRASTRUCTURE ONLY: the oracle the CUDA library is compared against,
 and the scalar CPU baseline of the benchmark.  Arrays use the reference's
 Fortran shapes in numpy Fortran order (state first; ro4 state last).
 """

@@ -1,7 +1,7 @@
 """CPU oracle of the NEVPT2 energy stage (stage 2 of the reference, QDnevpt2.x).
 
-TEST INFRASTRUCTURE ONLY: the checker of the CUDA stage-2 path and the scalar
-CPU baseline of the benchmark.  It restates src/qdnevpt.F for the
+TEST INFRASTRUCTURE ONLY: the reference the CUDA stage-2 path is tested against
+and the scalar CPU baseline of the benchmark.  It restates src/qdnevpt.F for the
 Cholesky-integral, C1 (nsym = 1) path that the synthetic configurations use:
 
   qdnevpt :369-698           core / virtual Fock operators and their
