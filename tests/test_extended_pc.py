@@ -31,3 +31,17 @@ def test_resolvent_form_equals_eigenpair_route(n, ne, nc, nv, M, seed):
         eld = X.plus2_pc_energy(inp, st, s, np.longdouble)
         assert abs(e64 - r.e2enp[3, s]) < 1e-12
         assert abs(float(eld) - r.e2enp[3, s]) < 1e-12
+
+
+def test_sensitivity_of_a_well_conditioned_class_is_at_rounding_level():
+    p = synth.make_problem(5, 4, 4, 5, metat=1, seed=6, with_ro4=False)
+    inp = X.stage2_inputs(p)
+    B, h = q.dense_B(inp.chol, inp.norb), q.unpack_tri(inp.oneint, inp.norb)
+    st = q._State(inp, 0, B, h)
+    e0 = X.plus2_pc_energy(inp, st, 0, np.float64, lapack=True)
+    sens = X.sensitivity(inp, st, 0)
+    assert set(sens) == {"eps_one_rounding", "eako2_one_rounding", "hrdm_one_rounding", "eako2_one_rounding_of_max"}
+    for v in sens.values():
+        assert 0.0 <= v < 1e-12 * max(1.0, abs(e0))
+    # the inputs are restored
+    assert X.plus2_pc_energy(inp, st, 0, np.float64, lapack=True) == e0
